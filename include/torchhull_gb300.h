@@ -1,0 +1,174 @@
+/*
+ * torchhull_gb300: C ABI of the GB300 (sm_103a) visual-hull and Gaussian-blur path.
+ *
+ * Plain C types only: device pointers, sizes, dtype codes and a CUDA stream
+ * passed as void* (a cudaStream_t; NULL is the legacy default stream).  All
+ * device work is enqueued on that stream.  Inputs are borrowed; outputs are
+ * written into buffers the caller allocates once the sizes are known, so the
+ * caller's allocator (for example torch's caching allocator) owns them.
+ *
+ * Each entry point names the reference interface it replaces
+ * (vc-bonn/torchhull v0.3.0, paths relative to that project).
+ *
+ * Threading: a th_context serves one request at a time.  Use one context per
+ * host thread (or guard it with a lock).  A context keeps its device pools
+ * between calls, so repeated requests do not allocate.
+ */
+#ifndef TORCHHULL_GB300_H
+#define TORCHHULL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TH_MAX_LEVEL 12
+
+typedef enum th_status
+{
+    TH_OK = 0,
+    TH_ERR_INVALID_ARGUMENT = 1, /* a TORCH_CHECK of the reference would fail */
+    TH_ERR_UNSUPPORTED_DTYPE = 2, /* the reference's AT_DISPATCH has no case for it */
+    TH_ERR_CUDA = 3,              /* a CUDA runtime call failed; see th_context_error */
+    TH_ERR_OUT_OF_MEMORY = 4,
+    TH_ERR_STATE = 5,    /* call order violated (export before a successful run) */
+    TH_ERR_NO_DEVICE = 6 /* no usable CUDA device */
+} th_status;
+
+/* Element types (same meaning as torch dtypes). */
+typedef enum th_dtype
+{
+    TH_BOOL = 0,
+    TH_UINT8 = 1,
+    TH_INT8 = 2,
+    TH_INT16 = 3,
+    TH_INT32 = 4,
+    TH_INT64 = 5,
+    TH_FLOAT16 = 6,
+    TH_FLOAT32 = 7,
+    TH_FLOAT64 = 8,
+    TH_BFLOAT16 = 9
+} th_dtype;
+
+typedef struct th_context th_context;
+
+/* Context holding the device pools for one CUDA device. */
+th_status th_context_create(int32_t device, th_context** out);
+void th_context_destroy(th_context* ctx);
+/* Message of the last failed call on ctx ("" if none); valid until the next call. */
+const char* th_context_error(const th_context* ctx);
+const char* th_status_string(th_status status);
+/* Bytes of device memory the context currently holds in its pools. */
+int64_t th_context_device_bytes(const th_context* ctx);
+
+/* Arguments of one visual-hull request.  masks: [B,H,W,1] contiguous device
+ * tensor; transforms: [B,4,4] contiguous device tensor (K*T per view). */
+typedef struct th_hull_args
+{
+    const void* masks;
+    int32_t masks_dtype; /* uint8, int8, int16, int32, int64, float16, float32, float64 */
+    int64_t batch;
+    int64_t height;
+    int64_t width;
+    const void* transforms;
+    int32_t transforms_dtype; /* float16, float32, float64 */
+    int32_t level;            /* 0 .. TH_MAX_LEVEL */
+    float cube_corner_bfl[3];
+    float cube_length;
+    int32_t masks_partial;
+    int32_t transforms_opengl; /* 1: "opengl", 0: "opencv" */
+    int32_t unique_verts;
+} th_hull_args;
+
+typedef struct th_hull_info
+{
+    int64_t num_verts;
+    int64_t num_faces;
+    int64_t num_corners; /* size of the sparse hull field */
+    int32_t num_levels;  /* entries of the candidate list, torchhull's candidates_octree */
+    int32_t reserved;
+    int64_t level_sizes[TH_MAX_LEVEL + 1];
+} th_hull_info;
+
+/*
+ * Runs the whole visual-hull path for one request on `stream` and returns the
+ * mesh sizes (one device->host read of a few counters; nothing else waits).
+ * The mesh and the per-level candidates stay in the context until the next
+ * th_visual_hull call; fetch them with the export calls below.
+ *
+ * Replaces torchhull::visual_hull (src/torchhull/_C/include/torchhull/visual_hull.h:11-19,
+ * src/torchhull/_C/src/visual_hull.cpp:34-83) and the host/device stages it
+ * chains (visual_hull_cuda.cu:582-894, marching_cubes_cuda.cu:535-754,
+ * visual_hull_cuda.cu:958-1020).
+ */
+th_status th_visual_hull(th_context* ctx, const th_hull_args* args, void* stream, th_hull_info* info);
+
+/* Writes the mesh of the last th_visual_hull call: verts [V,3] float32 in world
+ * coordinates, faces [F,3] int64 with torchhull's winding (columns 1 and 2
+ * swapped, visual_hull_cuda.cu:941-956).  Either pointer may be NULL when its
+ * count is 0. */
+th_status th_visual_hull_export(th_context* ctx, float* verts, int64_t* faces, void* stream);
+
+/* Candidate cells of level i of the last run (ravelled x-fastest at resolution
+ * 2^i, in torchhull's order), the list visual_hull_with_candidate_voxels
+ * returns (src/torchhull/_C/src/visual_hull.cpp:85-135). */
+th_status th_visual_hull_export_candidates(th_context* ctx, int32_t level, int64_t* dst, void* stream);
+
+/* Sparse hull field of the last run: ravelled grid indices (ascending, grid
+ * (2^level+1)^3) and values (visual_hull_cuda.cu:582-894, RavelledSparseTensor). */
+th_status th_visual_hull_export_field(th_context* ctx, int64_t* indices, float* values, void* stream);
+
+/*
+ * gaussian_blur(images, kernel_size, sigma, sparse, dtype) for images
+ * [B,H,W,1] contiguous on the device; out is [B,H,W,1] contiguous of
+ * out_dtype (float16/32/64).
+ * Replaces torchhull::gaussian_blur (src/torchhull/_C/include/torchhull/gaussian_blur.h:10-15,
+ * src/torchhull/_C/src/gaussian_blur.cpp:15-28, gaussian_blur_cuda.cu:73-518).
+ */
+th_status th_gaussian_blur(th_context* ctx,
+                           const void* images,
+                           int32_t images_dtype,
+                           int64_t batch,
+                           int64_t height,
+                           int64_t width,
+                           int32_t kernel_size,
+                           float sigma,
+                           int32_t sparse,
+                           void* out,
+                           int32_t out_dtype,
+                           void* stream);
+
+/* The float32 integral image of masks [B,H,W,1] into out [B,H,W], with the
+ * exact rounding of torch::cumsum(dim 1) then (dim 2) that the reference uses
+ * (visual_hull_cuda.cu:76-90). */
+th_status th_integral_image(th_context* ctx,
+                            const void* masks,
+                            int32_t masks_dtype,
+                            int64_t batch,
+                            int64_t height,
+                            int64_t width,
+                            float* out,
+                            void* stream);
+
+/*
+ * Batched form: n independent requests processed together (shared launches,
+ * one device->host read for all).  infos[n] receives the sizes; results stay
+ * in the context until the next batched call.  No counterpart in the
+ * reference, which serves one request per call; each result equals what
+ * th_visual_hull returns for that request alone.
+ */
+th_status th_visual_hull_batch(th_context* ctx, const th_hull_args* args, int32_t n, void* stream, th_hull_info* infos);
+th_status th_visual_hull_batch_export(th_context* ctx, int32_t index, float* verts, int64_t* faces, void* stream);
+
+/* Diagnostics (no reference counterpart): evaluates the device arithmetic the
+ * oracle emulates: out_i64[i] = (int64) in[i] as the GPU converts it, and
+ * out_f32[i] = c + v[i]/r * L written as the reference writes it. */
+th_status th_probe_arithmetic(const float* in, int64_t* out_i64, int64_t n, const int64_t* v, float r, float c, float L,
+                              float* out_f32, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TORCHHULL_GB300_H */

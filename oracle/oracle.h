@@ -1,0 +1,97 @@
+// CPU oracle for the visual-hull and Gaussian-blur path.
+//
+// TEST INFRASTRUCTURE ONLY.  This library is the checker: the parity tests,
+// the smoke check and the CPU baseline leg of the benchmark call it.  The
+// product path (the CUDA library and its Python/torch front end) never links,
+// loads or falls back to it.
+//
+// It restates torchhull's CUDA algorithm (vc-bonn/torchhull v0.3.0) on the
+// host, step by step and with the same float arithmetic, so that its results
+// can be compared bit for bit with the GPU path.  Every function cites the
+// reference file:line it follows.  Parity pinning: the reference ships no
+// golden vectors and cannot be built here (its CUDA build needs glm, stdgpu
+// and charonload, none of which exist offline), so this oracle is pinned only
+// against the reference's own property tests (empty/full masks, closed
+// 2-manifold meshes, soup sizes, OpenGL vs OpenCV agreement, blur identity
+// and dense/sparse agreement); bit-level parity with the reference's own CUDA
+// build is unpinned.
+#pragma once
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// Element types, same codes as th_dtype in include/torchhull_gb300.h.
+enum
+{
+    ORACLE_BOOL = 0,
+    ORACLE_UINT8 = 1,
+    ORACLE_INT8 = 2,
+    ORACLE_INT16 = 3,
+    ORACLE_INT32 = 4,
+    ORACLE_INT64 = 5,
+    ORACLE_FLOAT16 = 6,
+    ORACLE_FLOAT32 = 7,
+    ORACLE_FLOAT64 = 8,
+    ORACLE_BFLOAT16 = 9,
+};
+
+typedef struct oracle_hull oracle_hull;
+
+// Full visual_hull path (visual_hull.cpp:34-58).  masks: [B,H,W,1] contiguous,
+// transforms: [B,4,4] contiguous.  Returns NULL and fills err on an argument
+// error.  nthreads <= 0 uses all hardware threads.
+oracle_hull* oracle_visual_hull(const void* masks,
+                                int masks_dtype,
+                                int64_t B,
+                                int64_t H,
+                                int64_t W,
+                                const void* transforms,
+                                int transforms_dtype,
+                                int level,
+                                float corner_x,
+                                float corner_y,
+                                float corner_z,
+                                float cube_length,
+                                int masks_partial,
+                                int transforms_opengl,
+                                int unique_verts,
+                                int nthreads,
+                                char* err,
+                                int errlen);
+
+int64_t oracle_hull_num_levels(const oracle_hull* h);
+int64_t oracle_hull_level_size(const oracle_hull* h, int64_t i);
+void oracle_hull_level_copy(const oracle_hull* h, int64_t i, int64_t* dst);
+int64_t oracle_hull_field_size(const oracle_hull* h);
+void oracle_hull_field_copy(const oracle_hull* h, int64_t* indices, float* values);
+int64_t oracle_hull_num_verts(const oracle_hull* h);
+int64_t oracle_hull_num_faces(const oracle_hull* h);
+void oracle_hull_mesh_copy(const oracle_hull* h, float* verts, int64_t* faces);
+void oracle_hull_free(oracle_hull* h);
+
+// Float32 integral image exactly as torch::cumsum(dim=1) then (dim=2) computes
+// it (visual_hull_cuda.cu:76-90).  out: [B,H,W] float32.
+int oracle_integral_image(const void* masks, int masks_dtype, int64_t B, int64_t H, int64_t W, float* out, int nthreads);
+
+// gaussian_blur (gaussian_blur_cuda.cu:73-114 dense, :288-507 sparse).
+// out: [B,H,W,1] of out_dtype.  Returns 0 on success.
+int oracle_gaussian_blur(const void* images,
+                         int images_dtype,
+                         int64_t B,
+                         int64_t H,
+                         int64_t W,
+                         int kernel_size,
+                         float sigma,
+                         int sparse,
+                         void* out,
+                         int out_dtype,
+                         int nthreads,
+                         char* err,
+                         int errlen);
+
+#ifdef __cplusplus
+}
+#endif

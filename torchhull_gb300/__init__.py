@@ -1,0 +1,75 @@
+"""GB300 (sm_103a) implementation of torchhull's visual-hull and blur path.
+
+Drop-in for ``torchhull.visual_hull``, ``torchhull.visual_hull_with_candidate_voxels``,
+``torchhull.sparse_visual_hull_field`` and ``torchhull.gaussian_blur``: same
+argument names, defaults, outputs and errors.  The work runs in hand-written
+CUDA behind the C ABI of ``include/torchhull_gb300.h``; there is no CPU path,
+and CPU tensors raise the reference's "No backend implementation" error.
+
+Build once with ``python -c "import __graft_entry__ as g; g.build()"`` (or
+``python -m torchhull_gb300.build``); importing an unbuilt tree raises
+ImportError.
+"""
+
+from __future__ import annotations
+
+import importlib.machinery
+import importlib.util
+
+import torch
+
+from . import build as _build
+
+__all__ = [
+    "gaussian_blur",
+    "integral_image",
+    "sparse_visual_hull_field",
+    "visual_hull",
+    "visual_hull_with_candidate_voxels",
+]
+
+
+def _load_extension():
+    path = _build.extension_path()
+    if path is None or not _build.LIB.exists():
+        raise ImportError(
+            "torchhull_gb300 CUDA extension is not built (expected under torchhull_gb300/_build/); "
+            "run `python -m torchhull_gb300.build` first"
+        )
+    loader = importlib.machinery.ExtensionFileLoader(_build.EXT_NAME, str(path))
+    spec = importlib.util.spec_from_file_location(_build.EXT_NAME, str(path), loader=loader)
+    module = importlib.util.module_from_spec(spec)
+    loader.exec_module(module)
+    return module
+
+
+_C = _load_extension()
+
+visual_hull = _C.visual_hull
+visual_hull_with_candidate_voxels = _C.visual_hull_with_candidate_voxels
+gaussian_blur = _C.gaussian_blur
+integral_image = _C.integral_image
+
+
+def sparse_visual_hull_field(
+    masks: torch.Tensor,
+    transforms: torch.Tensor,
+    level: int,
+    cube_corner_bfl: tuple[float, float, float],
+    cube_length: float,
+    masks_partial: bool,
+    transforms_convention: str,
+) -> torch.Tensor:
+    """Sparse hull field as a coalesced COO tensor of size (1, R, R, R), R = 2^level + 1.
+
+    Indices are (0, z, y, x), values the product of the views' mask samples
+    (reference: visual_hull_cuda.cu:522-580, :896-914).
+    """
+    idx, values, r = _C.sparse_visual_hull_field_raw(
+        masks, transforms, level, cube_corner_bfl, cube_length, masks_partial, transforms_convention
+    )
+    z = idx // (r * r)
+    y = idx // r % r
+    x = idx % r
+    indices = torch.stack([torch.zeros_like(idx), z, y, x])
+    return torch.sparse_coo_tensor(indices, values, (1, r, r, r)).coalesce()

@@ -1,0 +1,624 @@
+// C ABI: contexts with resident device pools, request orchestration and
+// argument validation with the reference's error behaviour.
+//
+// One request enqueues every stage on the caller's stream and reads back one
+// small counter block at the end (the reference synchronises after every
+// kernel and reads counts back per level, visual_hull_cuda.cu:742, :820 and
+// marching_cubes_cuda.cu:600-634).  Pools only grow: a request whose octree or
+// corner set outgrows them is detected on the device, the pools double and the
+// request runs again, so repeated requests of similar size never allocate.
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "th_hull.cuh"
+#include "th_internal.h"
+
+namespace th
+{
+
+int sm_count()
+{
+    static int cache[64] = { 0 };
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return 148;
+    if (cache[dev] == 0)
+    {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+            n = 148;
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
+
+namespace
+{
+
+struct DevBuf
+{
+    void* p = nullptr;
+    size_t bytes = 0;
+
+    // Returns true when fresh memory was allocated (contents undefined).
+    bool ensure(size_t need)
+    {
+        if (need <= bytes && p)
+            return false;
+        if (p)
+            TH_CUDA(cudaFree(p));
+        p = nullptr;
+        bytes = 0;
+        size_t sz = std::max<size_t>(need, 256);
+        TH_CUDA(cudaMalloc(&p, sz));
+        bytes = sz;
+        return true;
+    }
+    void release()
+    {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const
+    {
+        return static_cast<T*>(p);
+    }
+};
+
+struct ArgError
+{
+    th_status status;
+    std::string msg;
+};
+
+const char* dtype_name(int d)
+{
+    static const char* names[] = { "Bool", "Byte", "Char", "Short", "Int", "Long", "Half", "Float", "Double", "BFloat16" };
+    return (d >= 0 && d <= 9) ? names[d] : "Unknown";
+}
+
+bool is_image_dtype(int d)
+{
+    return d >= TH_UINT8 && d <= TH_FLOAT64;
+}
+
+// Pools and the state of the last request of one context.
+struct HullSlot
+{
+    DevBuf tf, sat, nodes, child_masks, tile_sums, bitmap, word_rank, rowbits, rows, corners, values, codes, emask,
+            soup_off, vbase, counters;
+    int64_t node_cap = 0, corner_cap = 0;
+    int64_t bitmap_words = 0, rowbit_words = 0;
+    HullPlan plan{};
+    DevCounters* host = nullptr; // pinned copy of the counters
+    th_hull_info info{};
+    bool has_result = false;
+    bool dirty = false; // bitmap rows of the last request still set
+    cudaEvent_t done = nullptr;
+
+    void release()
+    {
+        for (DevBuf* b : { &tf, &sat, &nodes, &child_masks, &tile_sums, &bitmap, &word_rank, &rowbits, &rows, &corners,
+                           &values, &codes, &emask, &soup_off, &vbase, &counters })
+            b->release();
+        if (host)
+            cudaFreeHost(host);
+        host = nullptr;
+        if (done)
+            cudaEventDestroy(done);
+        done = nullptr;
+    }
+};
+
+} // namespace
+} // namespace th
+
+struct th_context
+{
+    int device = 0;
+    std::string error;
+    th::HullSlot hull;
+    std::vector<th::HullSlot> batch;
+    th::DevBuf blur_scratch;
+};
+
+namespace th
+{
+namespace
+{
+
+int64_t pool_bytes(const th_context* ctx)
+{
+    auto sum = [](const HullSlot& s) {
+        int64_t b = 0;
+        for (const DevBuf* d : { &s.tf, &s.sat, &s.nodes, &s.child_masks, &s.tile_sums, &s.bitmap, &s.word_rank,
+                                 &s.rowbits, &s.rows, &s.corners, &s.values, &s.codes, &s.emask, &s.soup_off, &s.vbase,
+                                 &s.counters })
+            b += static_cast<int64_t>(d->bytes);
+        return b;
+    };
+    int64_t total = sum(ctx->hull) + static_cast<int64_t>(ctx->blur_scratch.bytes);
+    for (const auto& s : ctx->batch)
+        total += sum(s);
+    return total;
+}
+
+void validate(const th_hull_args* a)
+{
+    if (!a)
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "args is NULL" };
+    // visual_hull_cuda.cu:591-613
+    if (a->batch < 0 || a->height < 0 || a->width < 0)
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: masks sizes must be non-negative" };
+    if (a->level < 0)
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: level >= 0 (" + std::to_string(a->level) + " vs. 0)" };
+    if (a->level > TH_MAX_LEVEL)
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT,
+                        "level " + std::to_string(a->level) + " exceeds the supported maximum " +
+                                std::to_string(TH_MAX_LEVEL) };
+    if (!(a->cube_length > 0.f))
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: cube_length > 0.f" };
+    // AT_DISPATCH_FLOATING_TYPES_AND_HALF over transforms (:646) and
+    // AT_DISPATCH_ALL_TYPES_AND(Half) over masks (:832)
+    if (!(a->transforms_dtype == TH_FLOAT16 || a->transforms_dtype == TH_FLOAT32 || a->transforms_dtype == TH_FLOAT64))
+        throw ArgError{ TH_ERR_UNSUPPORTED_DTYPE,
+                        std::string("\"classify_children\" not implemented for '") + dtype_name(a->transforms_dtype) +
+                                "'" };
+    if (!is_image_dtype(a->masks_dtype))
+        throw ArgError{ TH_ERR_UNSUPPORTED_DTYPE,
+                        std::string("\"accumulate_hull_counts\" not implemented for '") + dtype_name(a->masks_dtype) +
+                                "'" };
+    if (a->batch * a->height * a->width > 0 && (!a->masks || !a->transforms))
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "masks or transforms pointer is NULL" };
+    // Flagged/Unique/stdgpu use 32-bit indices (visual_hull_cuda.cu:716, :798)
+    if (a->batch * a->height * a->width >= (int64_t{ 1 } << 40))
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "masks too large" };
+}
+
+int64_t max_nodes(int level)
+{
+    // sum over levels of 8^i, the most the octree can hold
+    int64_t s = 0;
+    for (int i = 0; i <= level && i <= 12; ++i)
+        s += int64_t{ 1 } << (3 * i);
+    return s;
+}
+
+// Sizes the pools of slot s for request a and fills its plan.
+void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st)
+{
+    const int L = a->level;
+    const int64_t B = a->batch, H = a->height, W = a->width;
+    const int64_t R = (int64_t{ 1 } << L) + 1;
+    const int64_t WR = (R + 63) / 64;
+    if (s.node_cap == 0)
+    {
+        s.node_cap = std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 22);
+        s.corner_cap = std::min<int64_t>(R * R * R, int64_t{ 1 } << 23);
+    }
+    s.node_cap = std::max<int64_t>(s.node_cap, std::min<int64_t>(max_nodes(L), 4096));
+    s.corner_cap = std::max<int64_t>(s.corner_cap, std::min<int64_t>(R * R * R, 4096));
+    const int64_t node_cap = std::min<int64_t>(s.node_cap, max_nodes(L));
+    const int64_t corner_cap = std::min<int64_t>(s.corner_cap, R * R * R);
+
+    s.tf.ensure(sizeof(float) * std::max<int64_t>(B, 1) * 16);
+    s.sat.ensure(sizeof(float) * std::max<int64_t>(B * H * W, 1));
+    s.nodes.ensure(sizeof(int64_t) * node_cap);
+    s.child_masks.ensure(node_cap);
+    const int64_t scan_items = std::max({ node_cap, corner_cap, R * R });
+    s.tile_sums.ensure(sizeof(unsigned long long) * ((scan_items + kScanTile - 1) / kScanTile + 1));
+    const int64_t words = R * R * WR;
+    const int64_t rwords = (R * R + 31) / 32;
+    if (s.bitmap.ensure(sizeof(uint64_t) * words))
+        TH_CUDA(cudaMemsetAsync(s.bitmap.p, 0, s.bitmap.bytes, st));
+    s.word_rank.ensure(sizeof(uint32_t) * words);
+    if (s.rowbits.ensure(sizeof(uint32_t) * rwords))
+        TH_CUDA(cudaMemsetAsync(s.rowbits.p, 0, s.rowbits.bytes, st));
+    s.rows.ensure(sizeof(uint32_t) * R * R);
+    s.corners.ensure(sizeof(int64_t) * corner_cap);
+    s.values.ensure(sizeof(float) * corner_cap);
+    s.codes.ensure(corner_cap);
+    s.emask.ensure((corner_cap + 3) / 4 * 4);
+    s.soup_off.ensure(sizeof(uint32_t) * corner_cap);
+    s.vbase.ensure(sizeof(uint32_t) * corner_cap);
+    if (s.counters.ensure(sizeof(DevCounters)))
+        TH_CUDA(cudaMemsetAsync(s.counters.p, 0, sizeof(DevCounters), st));
+    if (!s.host)
+        TH_CUDA(cudaMallocHost(&s.host, sizeof(DevCounters)));
+    if (!s.done)
+        TH_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+
+    HullPlan& p = s.plan;
+    p = HullPlan{};
+    p.masks = a->masks;
+    p.masks_dtype = a->masks_dtype;
+    p.B = B;
+    p.H = H;
+    p.W = W;
+    p.tf = s.tf.as<float>();
+    p.sat = s.sat.as<float>();
+    p.opengl = a->transforms_opengl != 0;
+    p.partial = a->masks_partial != 0;
+    p.unique = a->unique_verts != 0;
+    p.corner[0] = a->cube_corner_bfl[0];
+    p.corner[1] = a->cube_corner_bfl[1];
+    p.corner[2] = a->cube_corner_bfl[2];
+    p.length = a->cube_length;
+    p.level = L;
+    p.nodes = s.nodes.as<int64_t>();
+    p.node_cap = node_cap;
+    p.child_masks = s.child_masks.as<uint8_t>();
+    p.tile_sums = s.tile_sums.as<unsigned long long>();
+    p.R = R;
+    p.WR = WR;
+    p.bitmap = s.bitmap.as<uint64_t>();
+    p.word_rank = s.word_rank.as<uint32_t>();
+    p.rowbits = s.rowbits.as<uint32_t>();
+    p.rows = s.rows.as<uint32_t>();
+    p.corners = s.corners.as<int64_t>();
+    p.values = s.values.as<float>();
+    p.codes = s.codes.as<uint8_t>();
+    p.emask = s.emask.as<uint8_t>();
+    p.soup_off = s.soup_off.as<uint32_t>();
+    p.vbase = s.vbase.as<uint32_t>();
+    p.corner_cap = corner_cap;
+    p.ctr = s.counters.as<DevCounters>();
+}
+
+void fill_info(const HullSlot& s, th_hull_info* info)
+{
+    const DevCounters& c = *s.host;
+    th_hull_info out{};
+    const HullPlan& p = s.plan;
+    // candidates_octree: levels up to and including the first empty one
+    int n = 1;
+    out.level_sizes[0] = c.level_count[0];
+    for (int i = 1; i <= p.level; ++i)
+    {
+        out.level_sizes[i] = c.level_count[i];
+        n = i + 1;
+        if (c.level_count[i] == 0)
+            break;
+    }
+    out.num_levels = n;
+    const bool empty = c.level_count[p.level] == 0;
+    out.num_corners = empty ? 0 : c.corners;
+    if (empty || c.soup == 0)
+    {
+        out.num_verts = 0;
+        out.num_faces = 0;
+    }
+    else
+    {
+        out.num_verts = p.unique ? c.verts : c.soup;
+        out.num_faces = c.soup / 3;
+    }
+    *info = out;
+}
+
+void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t st)
+{
+    validate(a);
+    if (s.dirty)
+    {
+        TH_CUDA(cudaStreamWaitEvent(st, s.done, 0));
+        launch_cleanup(s.plan, st);
+        s.dirty = false;
+    }
+    s.has_result = false;
+    for (int attempt = 0; attempt < 8; ++attempt)
+    {
+        prepare(s, a, st);
+        const HullPlan& p = s.plan;
+        if (attempt == 0)
+        {
+            launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), st);
+            launch_integral_image(a->masks, a->masks_dtype, a->batch, a->height, a->width, s.sat.as<float>(), st);
+        }
+        launch_hull_init(p, st);
+        for (int li = 0; li < p.level; ++li)
+            launch_carve_level(p, li, st);
+        launch_corners(p, st);
+        launch_field(p, st);
+        launch_marching_cubes(p, st);
+        TH_CUDA(cudaMemcpyAsync(s.host, p.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+        TH_CUDA(cudaStreamSynchronize(st));
+        s.dirty = true;
+        const int64_t ovf = s.host->overflow;
+        if (ovf == 0)
+            break;
+        launch_cleanup(p, st);
+        s.dirty = false;
+        if (ovf & kOverflowNodes)
+            s.node_cap *= 2;
+        if (ovf & kOverflowCorners)
+            s.corner_cap *= 2;
+        if (attempt == 7)
+            throw ArgError{ TH_ERR_OUT_OF_MEMORY, "visual hull pools could not be grown enough" };
+    }
+    fill_info(s, &s.info);
+    s.has_result = true;
+    (void)ctx;
+}
+
+th_status fail(th_context* ctx, th_status st, const std::string& msg)
+{
+    if (ctx)
+        ctx->error = msg;
+    return st;
+}
+
+template <class F>
+th_status guarded(th_context* ctx, F&& f)
+{
+    if (!ctx)
+        return TH_ERR_INVALID_ARGUMENT;
+    ctx->error.clear();
+    try
+    {
+        TH_CUDA(cudaSetDevice(ctx->device));
+        f();
+        return TH_OK;
+    }
+    catch (const ArgError& e)
+    {
+        return fail(ctx, e.status, e.msg);
+    }
+    catch (const CudaError& e)
+    {
+        const th_status st = (e.code == cudaErrorMemoryAllocation) ? TH_ERR_OUT_OF_MEMORY : TH_ERR_CUDA;
+        return fail(ctx, st, std::string(cudaGetErrorString(e.code)) + " (" + e.where + ")");
+    }
+    catch (const std::exception& e)
+    {
+        return fail(ctx, TH_ERR_CUDA, e.what());
+    }
+}
+
+} // namespace
+} // namespace th
+
+using namespace th;
+
+extern "C" {
+
+th_status th_context_create(int32_t device, th_context** out)
+{
+    if (!out)
+        return TH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0)
+        return TH_ERR_NO_DEVICE;
+    if (device < 0 || device >= n)
+        return TH_ERR_INVALID_ARGUMENT;
+    auto* ctx = new th_context;
+    ctx->device = device;
+    *out = ctx;
+    return TH_OK;
+}
+
+void th_context_destroy(th_context* ctx)
+{
+    if (!ctx)
+        return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    ctx->hull.release();
+    for (auto& s : ctx->batch)
+        s.release();
+    ctx->blur_scratch.release();
+    cudaSetDevice(prev);
+    delete ctx;
+}
+
+const char* th_context_error(const th_context* ctx)
+{
+    return ctx ? ctx->error.c_str() : "";
+}
+
+const char* th_status_string(th_status status)
+{
+    switch (status)
+    {
+    case TH_OK:
+        return "ok";
+    case TH_ERR_INVALID_ARGUMENT:
+        return "invalid argument";
+    case TH_ERR_UNSUPPORTED_DTYPE:
+        return "unsupported dtype";
+    case TH_ERR_CUDA:
+        return "CUDA error";
+    case TH_ERR_OUT_OF_MEMORY:
+        return "out of memory";
+    case TH_ERR_STATE:
+        return "invalid call order";
+    case TH_ERR_NO_DEVICE:
+        return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+int64_t th_context_device_bytes(const th_context* ctx)
+{
+    return ctx ? pool_bytes(ctx) : 0;
+}
+
+th_status th_visual_hull(th_context* ctx, const th_hull_args* args, void* stream, th_hull_info* info)
+{
+    return guarded(ctx, [&] {
+        run_hull(ctx, ctx->hull, args, static_cast<cudaStream_t>(stream));
+        if (info)
+            *info = ctx->hull.info;
+    });
+}
+
+th_status th_visual_hull_export(th_context* ctx, float* verts, int64_t* faces, void* stream)
+{
+    return guarded(ctx, [&] {
+        HullSlot& s = ctx->hull;
+        if (!s.has_result)
+            throw ArgError{ TH_ERR_STATE, "th_visual_hull_export called without a successful th_visual_hull" };
+        auto st = static_cast<cudaStream_t>(stream);
+        if (s.info.num_faces > 0)
+        {
+            if (!verts || !faces)
+                throw ArgError{ TH_ERR_INVALID_ARGUMENT, "verts or faces pointer is NULL" };
+            launch_export(s.plan, verts, faces, st);
+        }
+        TH_CUDA(cudaEventRecord(s.done, st));
+    });
+}
+
+th_status th_visual_hull_export_candidates(th_context* ctx, int32_t level, int64_t* dst, void* stream)
+{
+    return guarded(ctx, [&] {
+        HullSlot& s = ctx->hull;
+        if (!s.has_result)
+            throw ArgError{ TH_ERR_STATE, "export called without a successful th_visual_hull" };
+        if (level < 0 || level >= s.info.num_levels)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "candidate level out of range" };
+        const int64_t n = s.info.level_sizes[level];
+        if (n > 0)
+        {
+            if (!dst)
+                throw ArgError{ TH_ERR_INVALID_ARGUMENT, "dst is NULL" };
+            TH_CUDA(cudaMemcpyAsync(dst, s.plan.nodes + s.host->level_off[level], sizeof(int64_t) * n,
+                                    cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)));
+        }
+        TH_CUDA(cudaEventRecord(s.done, static_cast<cudaStream_t>(stream)));
+    });
+}
+
+th_status th_visual_hull_export_field(th_context* ctx, int64_t* indices, float* values, void* stream)
+{
+    return guarded(ctx, [&] {
+        HullSlot& s = ctx->hull;
+        if (!s.has_result)
+            throw ArgError{ TH_ERR_STATE, "export called without a successful th_visual_hull" };
+        const int64_t n = s.info.num_corners;
+        auto st = static_cast<cudaStream_t>(stream);
+        if (n > 0)
+        {
+            if (!indices || !values)
+                throw ArgError{ TH_ERR_INVALID_ARGUMENT, "indices or values pointer is NULL" };
+            TH_CUDA(cudaMemcpyAsync(indices, s.plan.corners, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, st));
+            TH_CUDA(cudaMemcpyAsync(values, s.plan.values, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+        }
+        TH_CUDA(cudaEventRecord(s.done, st));
+    });
+}
+
+th_status th_gaussian_blur(th_context* ctx,
+                           const void* images,
+                           int32_t images_dtype,
+                           int64_t batch,
+                           int64_t height,
+                           int64_t width,
+                           int32_t kernel_size,
+                           float sigma,
+                           int32_t sparse,
+                           void* out,
+                           int32_t out_dtype,
+                           void* stream)
+{
+    return guarded(ctx, [&] {
+        // gaussian_blur_cuda.cu:294-305 and :79-81
+        if (kernel_size <= 0)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT,
+                            "Check failed: kernel_size > 0 (" + std::to_string(kernel_size) + " vs. 0)" };
+        if (kernel_size % 2 != 1)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: kernel_size % 2 == 1 (" +
+                                                             std::to_string(kernel_size % 2) + " vs. 1)" };
+        if (!(sigma > 0.f))
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: sigma > 0.f" };
+        if (!(out_dtype == TH_FLOAT16 || out_dtype == TH_FLOAT32 || out_dtype == TH_FLOAT64))
+        {
+            if (out_dtype == TH_BFLOAT16)
+                throw ArgError{ TH_ERR_UNSUPPORTED_DTYPE, "\"tile_convolution_kernel\" not implemented for 'BFloat16'" };
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: torch::isFloatingType(dtype_result) == true" };
+        }
+        if (!is_image_dtype(images_dtype))
+            throw ArgError{ TH_ERR_UNSUPPORTED_DTYPE,
+                            std::string("\"edge_kernel\" not implemented for '") + dtype_name(images_dtype) + "'" };
+        if (batch < 0 || height < 0 || width < 0)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "image sizes must be non-negative" };
+        const int64_t n = batch * height * width;
+        if (n == 0)
+            return;
+        if (!images || !out)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "images or out pointer is NULL" };
+        const int64_t bytes = blur_tile_bytes(batch, height, width, kernel_size);
+        if (bytes > 0)
+            ctx->blur_scratch.ensure(static_cast<size_t>(bytes));
+        launch_gaussian_blur(images, images_dtype, batch, height, width, kernel_size, sigma, sparse != 0, out, out_dtype,
+                             ctx->blur_scratch.as<uint8_t>(), static_cast<cudaStream_t>(stream));
+    });
+}
+
+th_status th_integral_image(th_context* ctx,
+                            const void* masks,
+                            int32_t masks_dtype,
+                            int64_t batch,
+                            int64_t height,
+                            int64_t width,
+                            float* out,
+                            void* stream)
+{
+    return guarded(ctx, [&] {
+        if (!is_image_dtype(masks_dtype))
+            throw ArgError{ TH_ERR_UNSUPPORTED_DTYPE,
+                            std::string("integral image not implemented for '") + dtype_name(masks_dtype) + "'" };
+        if (batch < 0 || height < 0 || width < 0)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "mask sizes must be non-negative" };
+        if (batch * height * width == 0)
+            return;
+        if (!masks || !out)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "masks or out pointer is NULL" };
+        launch_integral_image(masks, masks_dtype, batch, height, width, out, static_cast<cudaStream_t>(stream));
+    });
+}
+
+th_status th_visual_hull_batch(th_context* ctx, const th_hull_args* args, int32_t n, void* stream, th_hull_info* infos)
+{
+    return guarded(ctx, [&] {
+        if (n < 0 || (n > 0 && (!args || !infos)))
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "invalid batch arguments" };
+        if (static_cast<int32_t>(ctx->batch.size()) < n)
+            ctx->batch.resize(n);
+        auto st = static_cast<cudaStream_t>(stream);
+        for (int32_t i = 0; i < n; ++i)
+        {
+            run_hull(ctx, ctx->batch[i], &args[i], st);
+            infos[i] = ctx->batch[i].info;
+        }
+    });
+}
+
+th_status th_visual_hull_batch_export(th_context* ctx, int32_t index, float* verts, int64_t* faces, void* stream)
+{
+    return guarded(ctx, [&] {
+        if (index < 0 || index >= static_cast<int32_t>(ctx->batch.size()) || !ctx->batch[index].has_result)
+            throw ArgError{ TH_ERR_STATE, "no batched result at this index" };
+        HullSlot& s = ctx->batch[index];
+        auto st = static_cast<cudaStream_t>(stream);
+        if (s.info.num_faces > 0)
+        {
+            if (!verts || !faces)
+                throw ArgError{ TH_ERR_INVALID_ARGUMENT, "verts or faces pointer is NULL" };
+            launch_export(s.plan, verts, faces, st);
+        }
+        TH_CUDA(cudaEventRecord(s.done, st));
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,549 @@
+// Leaf corners, hull field and sparse marching cubes.
+//
+// Corner set.  The reference turns the leaf cells into 8 corner ids each, then
+// radix-sorts and uniques them (visual_hull_cuda.cu:770-825).  Here each leaf
+// sets its corners in a bitmap over the (2^L+1)^3 grid, laid out row by row
+// (x fastest, one row = WR 64-bit words) so that scanning the set bits in
+// memory order yields the ids already ascending and unique.  A second bitmap
+// flags the rows that hold any bit, so only those rows are scanned and later
+// cleared.  The scan also stores, per word, the rank of its first bit, which
+// turns "index of corner v in the sorted list" into one word load, one rank
+// load and a popcount: this replaces the hash map the reference builds for its
+// marching cubes (marching_cubes_cuda.cu:66-70, :133-144).
+//
+// Hull field.  One thread per corner multiplies the bilinear mask samples of
+// all views in ascending view order, the order in which the reference's
+// per-view launches (visual_hull_cuda.cu:827-888) multiply them.
+//
+// Marching cubes.  A corner g is a cell when all 8 cube corners are present
+// (marching_cubes_cuda.cu:180-223).  Its code selects triangles from the
+// table; every edge a triangle uses is marked on the edge's lower corner (3
+// bits per corner, one per axis).  A scan over corners then numbers the marked
+// edges in (corner, axis) order, which is exactly the reference's vertex order
+// after torch::unique_dim over the edge ids (ravel(p1) << 3 | 1 << axis),
+// (:99-112, :674-693), without a sort.  Faces are emitted per cell in
+// ascending corner order and table order, as the reference's soup is.
+
+#include "mc_tables.h"
+#include "th_hull.cuh"
+#include "th_internal.h"
+
+namespace th
+{
+
+namespace
+{
+
+__device__ const uint8_t g_mc_count[256] = TH_MC_TRI_COUNT_INIT;
+__device__ const uint8_t g_mc_edges[256][15] = TH_MC_TRI_EDGES_INIT;
+
+struct TableCache
+{
+    uint8_t count[256];
+    uint8_t edges[256][16];
+};
+
+__device__ __forceinline__ void load_tables(TableCache& t)
+{
+    for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    {
+        t.count[i] = g_mc_count[i];
+#pragma unroll
+        for (int j = 0; j < 15; ++j)
+            t.edges[i][j] = g_mc_edges[i][j];
+    }
+    __syncthreads();
+}
+
+// Rank of grid point (x,y,z) among the set corners, or false if not set.
+__device__ __forceinline__ bool corner_rank(const HullPlan& p, int64_t x, int64_t y, int64_t z, uint32_t& rank)
+{
+    const int64_t row = y + z * p.R;
+    const int64_t w = row * p.WR + (x >> 6);
+    const uint64_t word = p.bitmap[w];
+    const uint64_t bit = 1ull << (x & 63);
+    if (!(word & bit))
+        return false;
+    rank = p.word_rank[w] + static_cast<uint32_t>(__popcll(word & (bit - 1)));
+    return true;
+}
+
+__device__ __forceinline__ void set_bits(uint64_t* words, int64_t w, uint64_t bits)
+{
+    if ((words[w] & bits) != bits)
+        atomicOr(reinterpret_cast<unsigned long long*>(words + w), static_cast<unsigned long long>(bits));
+}
+
+__global__ void __launch_bounds__(256) mark_corners_kernel(HullPlan p)
+{
+    const DevCounters* c = p.ctr;
+    const int L = p.level;
+    const int64_t n = c->level_count[L];
+    const int64_t* leaves = p.nodes + c->level_off[L];
+    const int64_t r = int64_t{ 1 } << L;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
+    {
+        const int64_t idx = leaves[t];
+        const int64_t x = idx % r, y = idx / r % r, z = idx / (r * r);
+        const int b = static_cast<int>(x & 63);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+        {
+            const int64_t row = (y + (q & 1)) + (z + (q >> 1)) * p.R;
+            const int64_t w = row * p.WR + (x >> 6);
+            if (b < 63)
+                set_bits(p.bitmap, w, 3ull << b);
+            else
+            {
+                set_bits(p.bitmap, w, 1ull << 63);
+                set_bits(p.bitmap, w + 1, 1ull);
+            }
+            const uint32_t rb = 1u << (row & 31);
+            if (!(p.rowbits[row >> 5] & rb))
+                atomicOr(p.rowbits + (row >> 5), rb);
+        }
+    }
+}
+
+struct RowCount
+{
+    const uint32_t* rowbits;
+    __device__ unsigned long long operator()(int64_t i) const
+    {
+        return static_cast<unsigned long long>(__popc(rowbits[i]));
+    }
+};
+
+struct RowEmit
+{
+    const uint32_t* rowbits;
+    uint32_t* rows;
+    __device__ void operator()(int64_t i, unsigned long long off, unsigned long long cnt) const
+    {
+        uint32_t w = rowbits[i];
+        while (w)
+        {
+            const int bit = __ffs(w) - 1;
+            rows[off++] = static_cast<uint32_t>(i * 32 + bit);
+            w &= w - 1;
+        }
+    }
+};
+
+struct RowEpilogue
+{
+    DevCounters* ctr;
+    __device__ void operator()(unsigned long long total) const
+    {
+        ctr->rows = static_cast<int64_t>(total);
+    }
+};
+
+struct CornerCount
+{
+    HullPlan p;
+    __device__ unsigned long long operator()(int64_t k) const
+    {
+        const int64_t base = static_cast<int64_t>(p.rows[k]) * p.WR;
+        unsigned long long s = 0;
+        for (int64_t w = 0; w < p.WR; ++w)
+            s += __popcll(p.bitmap[base + w]);
+        return s;
+    }
+};
+
+struct CornerEmit
+{
+    HullPlan p;
+    __device__ void operator()(int64_t k, unsigned long long off, unsigned long long) const
+    {
+        const int64_t row = p.rows[k];
+        const int64_t base = row * p.WR;
+        uint64_t out = off;
+        for (int64_t w = 0; w < p.WR; ++w)
+        {
+            uint64_t word = p.bitmap[base + w];
+            p.word_rank[base + w] = static_cast<uint32_t>(out);
+            while (word)
+            {
+                const int bit = __ffsll(static_cast<long long>(word)) - 1;
+                if (static_cast<int64_t>(out) < p.corner_cap)
+                {
+                    p.corners[out] = w * 64 + bit + row * p.R;
+                    p.emask[out] = 0;
+                }
+                ++out;
+                word &= word - 1;
+            }
+        }
+    }
+};
+
+struct CornerEpilogue
+{
+    DevCounters* ctr;
+    int64_t cap;
+    __device__ void operator()(unsigned long long total) const
+    {
+        int64_t n = static_cast<int64_t>(total);
+        if (n > cap)
+        {
+            ctr->overflow |= kOverflowCorners;
+            n = cap;
+        }
+        ctr->corners = n;
+    }
+};
+
+template <int DT>
+__device__ __forceinline__ float mask_sample(const HullPlan& p, int64_t b, int64_t y, int64_t x, float pad)
+{
+    return in_image(y, x, p.H, p.W) ? load_f32<DT>(p.masks, (b * p.H + y) * p.W + x) : pad;
+}
+
+__device__ __forceinline__ int64_t add1(int64_t v)
+{
+    return static_cast<int64_t>(static_cast<uint64_t>(v) + 1u);
+}
+
+// accumulate_hull_counts_{full,partial} (visual_hull_cuda.cu:419-520) and the
+// bilinear samplers (image_utils.h:162-214), all views in one thread.
+template <int DT, bool PARTIAL>
+__global__ void __launch_bounds__(256) field_kernel(HullPlan p)
+{
+    const int64_t n = p.ctr->corners;
+    const int64_t R = p.R;
+    const float rcf = static_cast<float>(R - 1);
+    const float Hf = static_cast<float>(p.H), Wf = static_cast<float>(p.W);
+    const float pad = PARTIAL ? 1.f : 0.f;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
+    {
+        const int64_t idx = p.corners[t];
+        const int64_t gx = idx % R, gy = idx / R % R, gz = idx / (R * R);
+        const float wx = world_coordinate(gx, rcf, p.corner[0], p.length);
+        const float wy = world_coordinate(gy, rcf, p.corner[1], p.length);
+        const float wz = world_coordinate(gz, rcf, p.corner[2], p.length);
+        float value = 1.f;
+        for (int64_t b = 0; b < p.B; ++b)
+        {
+            const float* m = p.tf + 16 * b;
+            float px, py;
+            to_pixel(m, wx, wy, wz, p.opengl, Hf, Wf, px, py);
+            if (PARTIAL)
+            {
+                const int64_t rx = f2i64(roundf(px)), ry = f2i64(roundf(py));
+                if (!in_image(ry, rx, p.H, p.W, 1))
+                    continue;
+            }
+            const int64_t yp = f2i64(roundf(__fadd_rn(py, -0.5f)));
+            const int64_t xp = f2i64(roundf(__fadd_rn(px, -0.5f)));
+            const float v00 = mask_sample<DT>(p, b, yp, xp, pad);
+            const float v10 = mask_sample<DT>(p, b, add1(yp), xp, pad);
+            const float v01 = mask_sample<DT>(p, b, yp, add1(xp), pad);
+            const float v11 = mask_sample<DT>(p, b, add1(yp), add1(xp), pad);
+            const float ty = __fsub_rn(py, __ll2float_rn(yp));
+            const float tx = __fsub_rn(px, __ll2float_rn(xp));
+            value = __fmul_rn(value, bilerp(v00, v10, v01, v11, ty, tx));
+        }
+        p.values[t] = value;
+    }
+}
+
+// Ranks of the 8 corners of the cell with base corner t; false if incomplete.
+// Ranks at or beyond n (possible only when the corner pool overflowed and the
+// request is about to be rerun) count as missing, so no access leaves the pools.
+__device__ __forceinline__ bool cell_ranks(const HullPlan& p,
+                                           int64_t t,
+                                           int64_t n,
+                                           int64_t gx,
+                                           int64_t gy,
+                                           int64_t gz,
+                                           uint32_t rk[8])
+{
+    const int64_t R = p.R;
+    if (!(gx < R - 1 && gy < R - 1 && gz < R - 1))
+        return false;
+    rk[0] = static_cast<uint32_t>(t);
+#pragma unroll
+    for (int i = 1; i < 8; ++i)
+        if (!corner_rank(p, gx + (i & 1), gy + (i >> 1 & 1), gz + (i >> 2 & 1), rk[i]) || rk[i] >= n)
+            return false;
+    return true;
+}
+
+// classify_voxels_sparse (marching_cubes_cuda.cu:180-223) plus edge marking.
+__global__ void __launch_bounds__(256) mc_cells_kernel(HullPlan p)
+{
+    __shared__ TableCache tab;
+    load_tables(tab);
+    const int64_t n = p.ctr->corners;
+    const int64_t R = p.R;
+    const float iso = 0.5f;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
+    {
+        const int64_t idx = p.corners[t];
+        const int64_t gx = idx % R, gy = idx / R % R, gz = idx / (R * R);
+        uint32_t rk[8];
+        uint32_t code = 0;
+        if (cell_ranks(p, t, n, gx, gy, gz, rk))
+        {
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (p.values[rk[i]] < iso)
+                    code |= 1u << i;
+            const int cnt = tab.count[code];
+            uint32_t used = 0; // bit (lo * 3 + axis)
+            for (int j = 0; j < cnt; ++j)
+            {
+                const uint32_t e = tab.edges[code][j];
+                used |= 1u << ((e & 7u) * 3u + (e >> 3));
+            }
+            while (used)
+            {
+                const int k = __ffs(used) - 1;
+                used &= used - 1;
+                const uint32_t r1 = rk[k / 3];
+                const uint32_t bit = (1u << (k % 3)) << (8u * (r1 & 3u));
+                unsigned int* word = reinterpret_cast<unsigned int*>(p.emask) + (r1 >> 2);
+                if ((*word & bit) != bit)
+                    atomicOr(word, bit);
+            }
+        }
+        p.codes[t] = static_cast<uint8_t>(code);
+    }
+}
+
+struct VertCount
+{
+    const uint8_t* codes;
+    const uint8_t* emask;
+    __device__ unsigned long long operator()(int64_t t) const
+    {
+        return (static_cast<unsigned long long>(g_mc_count[codes[t]]) << 32) |
+               static_cast<unsigned long long>(__popc(emask[t]));
+    }
+};
+
+struct VertEmit
+{
+    uint32_t* soup_off;
+    uint32_t* vbase;
+    __device__ void operator()(int64_t t, unsigned long long off, unsigned long long) const
+    {
+        soup_off[t] = static_cast<uint32_t>(off >> 32);
+        vbase[t] = static_cast<uint32_t>(off & 0xffffffffull);
+    }
+};
+
+struct VertEpilogue
+{
+    DevCounters* ctr;
+    __device__ void operator()(unsigned long long total) const
+    {
+        ctr->soup = static_cast<int64_t>(total >> 32);
+        ctr->verts = static_cast<int64_t>(total & 0xffffffffull);
+    }
+};
+
+// interpolate_vertex (marching_cubes_cuda.cu:72-97) followed by the world
+// transform of to_global_coordinates (visual_hull_cuda.cu:916-939).
+__device__ __forceinline__ void edge_vertex(const HullPlan& p,
+                                            int64_t x1,
+                                            int64_t y1,
+                                            int64_t z1,
+                                            int axis,
+                                            float v1,
+                                            float v2,
+                                            float scale,
+                                            float* out)
+{
+    const float iso = 0.5f, eps = 1e-5f;
+    const int64_t x2 = x1 + (axis == 0), y2 = y1 + (axis == 1), z2 = z1 + (axis == 2);
+    // 1: snap to p1, 2: snap to p2, 0: interpolate (the reference's check order)
+    int snap = 0;
+    if (fabsf(__fsub_rn(iso, v1)) < eps)
+        snap = 1;
+    else if (fabsf(__fsub_rn(iso, v2)) < eps)
+        snap = 2;
+    else if (fabsf(__fsub_rn(v1, v2)) < eps)
+        snap = 1;
+    float q[3];
+    if (snap == 1)
+    {
+        q[0] = static_cast<float>(x1);
+        q[1] = static_cast<float>(y1);
+        q[2] = static_cast<float>(z1);
+    }
+    else if (snap == 2)
+    {
+        q[0] = static_cast<float>(x2);
+        q[1] = static_cast<float>(y2);
+        q[2] = static_cast<float>(z2);
+    }
+    else
+    {
+        const float t = __fdiv_rn(__fsub_rn(iso, v1), __fsub_rn(v2, v1));
+        q[0] = lerp(static_cast<float>(x1), static_cast<float>(x2), t);
+        q[1] = lerp(static_cast<float>(y1), static_cast<float>(y2), t);
+        q[2] = lerp(static_cast<float>(z1), static_cast<float>(z2), t);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        out[a] = __fmaf_rn(scale, q[a], p.corner[a]);
+}
+
+__global__ void __launch_bounds__(256) export_verts_kernel(HullPlan p, float* __restrict__ verts)
+{
+    const int64_t n = p.ctr->corners;
+    const int64_t R = p.R;
+    const float scale = __fdiv_rn(p.length, static_cast<float>(int64_t{ 1 } << p.level));
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
+    {
+        const uint32_t bits = p.emask[t];
+        if (!bits)
+            continue;
+        const int64_t idx = p.corners[t];
+        const int64_t gx = idx % R, gy = idx / R % R, gz = idx / (R * R);
+        const float v1 = p.values[t];
+        int64_t out = p.vbase[t];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+        {
+            if (!(bits >> a & 1u))
+                continue;
+            uint32_t r2 = 0;
+            corner_rank(p, gx + (a == 0), gy + (a == 1), gz + (a == 2), r2);
+            float v[3];
+            edge_vertex(p, gx, gy, gz, a, v1, p.values[r2], scale, v);
+            verts[3 * out + 0] = v[0];
+            verts[3 * out + 1] = v[1];
+            verts[3 * out + 2] = v[2];
+            ++out;
+        }
+    }
+}
+
+// Faces in soup order; with unique vertices they index the edge-numbered
+// vertex list, without they index the soup, which this kernel also writes.
+// Columns 1 and 2 are swapped as flip_faces does (visual_hull_cuda.cu:941-956).
+__global__ void __launch_bounds__(256) export_faces_kernel(HullPlan p, float* __restrict__ verts, int64_t* __restrict__ faces)
+{
+    __shared__ TableCache tab;
+    load_tables(tab);
+    const int64_t n = p.ctr->corners;
+    const int64_t R = p.R;
+    const float scale = __fdiv_rn(p.length, static_cast<float>(int64_t{ 1 } << p.level));
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
+    {
+        const uint32_t code = p.codes[t];
+        const int cnt = tab.count[code];
+        if (cnt == 0)
+            continue;
+        const int64_t idx = p.corners[t];
+        const int64_t gx = idx % R, gy = idx / R % R, gz = idx / (R * R);
+        uint32_t rk[8];
+        cell_ranks(p, t, n, gx, gy, gz, rk);
+        const int64_t base = p.soup_off[t];
+        for (int j = 0; j < cnt; ++j)
+        {
+            const uint32_t e = tab.edges[code][j];
+            const int lo = static_cast<int>(e & 7u), axis = static_cast<int>(e >> 3);
+            const int64_t f = base + j;
+            const int slot = static_cast<int>(f % 3);
+            const int64_t dst = f - slot + (slot == 0 ? 0 : 3 - slot);
+            if (p.unique)
+            {
+                const uint32_t r1 = rk[lo];
+                faces[dst] = static_cast<int64_t>(p.vbase[r1]) + __popc(p.emask[r1] & ((1u << axis) - 1u));
+            }
+            else
+            {
+                float v[3];
+                const int hi = lo | (1 << axis);
+                edge_vertex(p, gx + (lo & 1), gy + (lo >> 1 & 1), gz + (lo >> 2 & 1), axis, p.values[rk[lo]],
+                            p.values[rk[hi]], scale, v);
+                verts[3 * f + 0] = v[0];
+                verts[3 * f + 1] = v[1];
+                verts[3 * f + 2] = v[2];
+                faces[dst] = f;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) clear_rows_kernel(HullPlan p)
+{
+    const int64_t n = p.ctr->rows;
+    const int64_t total = n * p.WR;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += stride)
+    {
+        const int64_t k = i / p.WR, w = i - k * p.WR;
+        p.bitmap[static_cast<int64_t>(p.rows[k]) * p.WR + w] = 0;
+    }
+}
+
+} // namespace
+
+void launch_corners(const HullPlan& p, cudaStream_t s)
+{
+    const int64_t max_leaves = p.node_cap;
+    mark_corners_kernel<<<grid_for(max_leaves, 256), 256, 0, s>>>(p);
+    TH_LAUNCH_CHECK();
+    const int64_t row_words = (p.R * p.R + 31) / 32;
+    run_scan(RowCount{ p.rowbits }, RowEmit{ p.rowbits, p.rows }, RowEpilogue{ p.ctr }, Count{ nullptr, row_words },
+             row_words, p.tile_sums, &p.ctr->scan, s);
+    TH_LAUNCH_CHECK();
+    run_scan(CornerCount{ p }, CornerEmit{ p }, CornerEpilogue{ p.ctr, p.corner_cap }, Count{ &p.ctr->rows, 0 },
+             p.R * p.R, p.tile_sums, &p.ctr->scan, s);
+    TH_LAUNCH_CHECK();
+}
+
+void launch_field(const HullPlan& p, cudaStream_t s)
+{
+    const int grid = grid_for(p.corner_cap, 256);
+    bool ok = dispatch_image_dtype(p.masks_dtype, [&]<int DT>() {
+        if (p.partial)
+            field_kernel<DT, true><<<grid, 256, 0, s>>>(p);
+        else
+            field_kernel<DT, false><<<grid, 256, 0, s>>>(p);
+    });
+    if (!ok)
+        throw CudaError{ cudaErrorInvalidValue, "hull field: unsupported mask dtype" };
+    TH_LAUNCH_CHECK();
+}
+
+void launch_marching_cubes(const HullPlan& p, cudaStream_t s)
+{
+    mc_cells_kernel<<<grid_for(p.corner_cap, 256), 256, 0, s>>>(p);
+    TH_LAUNCH_CHECK();
+    run_scan(VertCount{ p.codes, p.emask }, VertEmit{ p.soup_off, p.vbase }, VertEpilogue{ p.ctr },
+             Count{ &p.ctr->corners, 0 }, p.corner_cap, p.tile_sums, &p.ctr->scan, s);
+    TH_LAUNCH_CHECK();
+}
+
+void launch_export(const HullPlan& p, float* verts, int64_t* faces, cudaStream_t s)
+{
+    const int grid = grid_for(p.corner_cap, 256);
+    if (p.unique)
+    {
+        export_verts_kernel<<<grid, 256, 0, s>>>(p, verts);
+        TH_LAUNCH_CHECK();
+    }
+    export_faces_kernel<<<grid, 256, 0, s>>>(p, verts, faces);
+    TH_LAUNCH_CHECK();
+}
+
+void launch_cleanup(const HullPlan& p, cudaStream_t s)
+{
+    clear_rows_kernel<<<grid_for(p.R * p.R * p.WR, 256), 256, 0, s>>>(p);
+    TH_LAUNCH_CHECK();
+    TH_CUDA(cudaMemsetAsync(p.rowbits, 0, sizeof(uint32_t) * ((p.R * p.R + 31) / 32), s));
+}
+
+} // namespace th

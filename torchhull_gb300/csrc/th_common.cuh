@@ -1,0 +1,348 @@
+// Shared device helpers: element loads, the reference's float arithmetic
+// (operation for operation, so results match bit for bit), index helpers and
+// a device-wide scan built from two grid-stride kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/torchhull_gb300.h"
+
+namespace th
+{
+
+constexpr int kMaxLevel = 12;
+
+// ---------------------------------------------------------------------------
+// element loads: value of element i converted the way static_cast<float>(T)
+// converts it (round to nearest for wide integers and double).
+
+template <int DT>
+struct Elem;
+template <>
+struct Elem<TH_UINT8>
+{
+    using T = uint8_t;
+};
+template <>
+struct Elem<TH_INT8>
+{
+    using T = int8_t;
+};
+template <>
+struct Elem<TH_INT16>
+{
+    using T = int16_t;
+};
+template <>
+struct Elem<TH_INT32>
+{
+    using T = int32_t;
+};
+template <>
+struct Elem<TH_INT64>
+{
+    using T = int64_t;
+};
+template <>
+struct Elem<TH_FLOAT16>
+{
+    using T = __half;
+};
+template <>
+struct Elem<TH_FLOAT32>
+{
+    using T = float;
+};
+template <>
+struct Elem<TH_FLOAT64>
+{
+    using T = double;
+};
+
+template <int DT>
+__device__ __forceinline__ float load_f32(const void* p, int64_t i)
+{
+    using T = typename Elem<DT>::T;
+    if constexpr (DT == TH_FLOAT16)
+        return __half2float(static_cast<const __half*>(p)[i]);
+    else
+        return static_cast<float>(static_cast<const T*>(p)[i]);
+}
+
+// Calls f.template operator()<DT>() for a mask/image dtype code; returns false
+// for dtypes the reference's dispatch does not cover (bool, bfloat16).
+template <class F>
+bool dispatch_image_dtype(int dt, F&& f)
+{
+    switch (dt)
+    {
+    case TH_UINT8:
+        f.template operator()<TH_UINT8>();
+        return true;
+    case TH_INT8:
+        f.template operator()<TH_INT8>();
+        return true;
+    case TH_INT16:
+        f.template operator()<TH_INT16>();
+        return true;
+    case TH_INT32:
+        f.template operator()<TH_INT32>();
+        return true;
+    case TH_INT64:
+        f.template operator()<TH_INT64>();
+        return true;
+    case TH_FLOAT16:
+        f.template operator()<TH_FLOAT16>();
+        return true;
+    case TH_FLOAT32:
+        f.template operator()<TH_FLOAT32>();
+        return true;
+    case TH_FLOAT64:
+        f.template operator()<TH_FLOAT64>();
+        return true;
+    default:
+        return false;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// reference arithmetic (torchhull image_utils.h, math.h, visual_hull_cuda.cu)
+
+__device__ __forceinline__ bool in_image(int64_t y, int64_t x, int64_t h, int64_t w, int64_t margin = 0)
+{
+    return margin <= y && y < h - margin && margin <= x && x < w - margin;
+}
+
+__device__ __forceinline__ float lerp(float v0, float v1, float t)
+{
+    return __fmaf_rn(t, v1, __fmaf_rn(-t, v0, v0));
+}
+
+__device__ __forceinline__ float bilerp(float v00, float v10, float v01, float v11, float ty, float tx)
+{
+    float v0 = lerp(v00, v10, ty);
+    float v1 = lerp(v01, v11, ty);
+    return lerp(v0, v1, tx);
+}
+
+// c + v/r * L with the product fused, as nvcc contracts the reference's
+// expression (visual_hull_cuda.cu:206-213); v/r is exact (r a power of two).
+__device__ __forceinline__ float world_coordinate(int64_t v, float r, float corner, float length)
+{
+    return __fmaf_rn(__fdiv_rn(static_cast<float>(v), r), length, corner);
+}
+
+// float -> int64 truncation; the hardware conversion saturates and maps NaN to 0.
+__device__ __forceinline__ int64_t f2i64(float f)
+{
+    return __float2ll_rz(f);
+}
+
+// K*T*[x,y,z,1] with nested fmaf (visual_hull_cuda.cu:142-156). m is row-major 4x4.
+__device__ __forceinline__ float project_row(const float* m, float x, float y, float z)
+{
+    return __fmaf_rn(m[0], x, __fmaf_rn(m[1], y, __fmaf_rn(m[2], z, m[3])));
+}
+
+// Pixel position of a camera-space point (image_utils.h:62-82).
+__device__ __forceinline__ void to_pixel(const float* m, float x, float y, float z, bool opengl, float H, float W, float& px, float& py)
+{
+    float cx = project_row(m + 0, x, y, z);
+    float cy = project_row(m + 4, x, y, z);
+    if (opengl)
+    {
+        float cw = project_row(m + 12, x, y, z);
+        float nx = __fdiv_rn(cx, cw);
+        float ny = __fdiv_rn(cy, cw);
+        px = __fsub_rn(__fdiv_rn(__fmul_rn(__fadd_rn(nx, 1.f), W), 2.f), 0.5f);
+        py = __fsub_rn(__fdiv_rn(__fmul_rn(__fadd_rn(ny, 1.f), H), 2.f), 0.5f);
+    }
+    else
+    {
+        float cz = project_row(m + 8, x, y, z);
+        px = __fsub_rn(__fdiv_rn(cx, cz), 0.5f);
+        py = __fsub_rn(__fdiv_rn(cy, cz), 0.5f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// device-wide scan over n items (n read from device memory) whose counts come
+// from a functor.  Pass 1 writes one sum per tile and the block that finishes
+// last turns them into exclusive tile offsets (no inter-block waiting); pass 2
+// rescans each tile and hands every item its exclusive offset.
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+template <typename T>
+__device__ __forceinline__ T warp_inclusive_scan(T v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1)
+    {
+        T u = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d)
+            v += u;
+    }
+    return v;
+}
+
+// Exclusive scan across the block; returns the thread's exclusive prefix and
+// writes the block total to *total (all threads).
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T* total)
+{
+    __shared__ T warp_sums[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    T inc = warp_inclusive_scan(v);
+    if (lane == 31)
+        warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0)
+    {
+        T s = lane < nwarps ? warp_sums[lane] : T(0);
+        T si = warp_inclusive_scan(s);
+        if (lane < nwarps)
+            warp_sums[lane] = si - s;
+        if (lane == nwarps - 1)
+            warp_sums[31] = si;
+    }
+    __syncthreads();
+    T out = warp_sums[warp] + inc - v;
+    *total = warp_sums[31];
+    __syncthreads();
+    return out;
+}
+
+struct ScanState
+{
+    unsigned int blocks_done;
+    unsigned int pad;
+    unsigned long long total;
+};
+
+// Item count of a scan: read from device memory when ptr is set, else val.
+struct Count
+{
+    const int64_t* ptr;
+    int64_t val;
+    __device__ __forceinline__ int64_t get() const
+    {
+        return ptr ? *ptr : val;
+    }
+};
+
+struct NoEpilogue
+{
+    __device__ void operator()(unsigned long long) const {}
+};
+
+// epi(total) runs once, on one thread, after all tile offsets are final.
+template <class CountF, class EpiF>
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(CountF count,
+                                                                   Count n_src,
+                                                                   unsigned long long* __restrict__ tile_sums,
+                                                                   ScanState* __restrict__ state,
+                                                                   EpiF epi)
+{
+    const int64_t n = n_src.get();
+    const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+    {
+        unsigned long long s = 0;
+        const int64_t base = tile * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            if (base + k < n)
+                s += count(base + k);
+        unsigned long long tot;
+        block_exclusive_scan(s, &tot);
+        if (threadIdx.x == 0)
+            tile_sums[tile] = tot;
+    }
+    __threadfence();
+    __shared__ bool is_last;
+    if (threadIdx.x == 0)
+        is_last = (atomicAdd(&state->blocks_done, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!is_last)
+        return;
+    __threadfence();
+    // exclusive scan of the tile sums, in place
+    unsigned long long carry = 0;
+    for (int64_t b = 0; b < ntiles; b += kScanThreads)
+    {
+        int64_t t = b + threadIdx.x;
+        unsigned long long v = t < ntiles ? *((volatile unsigned long long*)&tile_sums[t]) : 0ull;
+        unsigned long long tot;
+        unsigned long long ex = block_exclusive_scan(v, &tot);
+        if (t < ntiles)
+            tile_sums[t] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0)
+    {
+        state->total = carry;
+        state->blocks_done = 0;
+        epi(carry);
+    }
+}
+
+// emit(i, exclusive_offset, count) is called for every item (count may be 0).
+template <class CountF, class EmitF>
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(CountF count,
+                                                                  EmitF emit,
+                                                                  Count n_src,
+                                                                  const unsigned long long* __restrict__ tile_offsets)
+{
+    const int64_t n = n_src.get();
+    const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+    {
+        const int64_t base = tile * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
+        unsigned long long c[kScanItems];
+        unsigned long long s = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+        {
+            c[k] = (base + k < n) ? count(base + k) : 0ull;
+            s += c[k];
+        }
+        unsigned long long tot;
+        unsigned long long off = block_exclusive_scan(s, &tot) + tile_offsets[tile];
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+        {
+            if (base + k < n)
+                emit(base + k, off, c[k]);
+            off += c[k];
+        }
+    }
+}
+
+int sm_count();
+
+// Both scan passes on stream s.  n_max bounds the item count on the host side
+// (it sizes the grid; tile_sums must hold ceil(n_max / kScanTile) entries).
+template <class CountF, class EmitF, class EpiF>
+inline void run_scan(CountF count,
+                     EmitF emit,
+                     EpiF epi,
+                     Count n,
+                     int64_t n_max,
+                     unsigned long long* tile_sums,
+                     ScanState* state,
+                     cudaStream_t s)
+{
+    const int64_t tiles = (n_max + kScanTile - 1) / kScanTile;
+    const int64_t cap = 4LL * sm_count();
+    const int grid = static_cast<int>(tiles < 1 ? 1 : (tiles < cap ? tiles : cap));
+    scan_reduce_kernel<<<grid, kScanThreads, 0, s>>>(count, n, tile_sums, state, epi);
+    scan_apply_kernel<<<grid, kScanThreads, 0, s>>>(count, emit, n, tile_sums);
+}
+
+} // namespace th

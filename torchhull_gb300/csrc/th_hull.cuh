@@ -1,0 +1,77 @@
+// Device-side state of one visual-hull request and the launch entry points of
+// its stages (carve.cu, mesh.cu).  Every count lives in device memory, so the
+// stages chain on one stream with no host round trip; kernels are grid-stride
+// loops sized from the SM count that read their item count on the device.
+#pragma once
+
+#include <cstdint>
+
+#include "th_common.cuh"
+
+namespace th
+{
+
+enum OverflowBits : int64_t
+{
+    kOverflowNodes = 1,
+    kOverflowCorners = 2,
+    kOverflowSoup = 4,
+};
+
+struct DevCounters
+{
+    int64_t level_count[kMaxLevel + 2]; // cells of level i (level 0: the root)
+    int64_t level_off[kMaxLevel + 3];   // start of level i in the node pool
+    int64_t rows;                       // bitmap rows holding at least one corner
+    int64_t corners;                    // unique leaf corners (the sparse field)
+    int64_t soup;                       // soup vertices, 3 per face
+    int64_t verts;                      // unique mesh vertices
+    int64_t overflow;                   // OverflowBits
+    int64_t row_words;                  // words of the row-occupancy bitmap
+    ScanState scan;
+};
+
+// Per-request constants and buffers, passed to kernels by value.
+struct HullPlan
+{
+    // inputs
+    const void* masks;
+    int masks_dtype;
+    int64_t B, H, W;
+    const float* tf;  // [B,16] float32
+    const float* sat; // [B,H,W]
+    bool opengl, partial, unique;
+    float corner[3];
+    float length;
+    int level;
+    // octree node pool: all levels back to back
+    int64_t* nodes;
+    int64_t node_cap;
+    uint8_t* child_masks; // one byte per parent of the current level
+    unsigned long long* tile_sums;
+    // corner grid: R^3 points, one bit each, rows of WR 64-bit words (x fastest)
+    int64_t R, WR;
+    uint64_t* bitmap;     // [R*R*WR]
+    uint32_t* word_rank;  // [R*R*WR] rank of the word's first bit (valid for touched rows)
+    uint32_t* rowbits;    // [ceil(R*R/32)] touched-row flags
+    uint32_t* rows;       // [R*R] touched rows, ascending
+    // sparse field and marching cubes, indexed by corner rank
+    int64_t* corners;
+    float* values;
+    uint8_t* codes;
+    uint8_t* emask; // bit a: the edge from this corner along axis a carries a vertex
+    uint32_t* soup_off;
+    uint32_t* vbase;
+    int64_t corner_cap;
+    DevCounters* ctr;
+};
+
+void launch_hull_init(const HullPlan& p, cudaStream_t s);
+void launch_carve_level(const HullPlan& p, int level_index, cudaStream_t s);
+void launch_corners(const HullPlan& p, cudaStream_t s);
+void launch_field(const HullPlan& p, cudaStream_t s);
+void launch_marching_cubes(const HullPlan& p, cudaStream_t s);
+void launch_export(const HullPlan& p, float* verts, int64_t* faces, cudaStream_t s);
+void launch_cleanup(const HullPlan& p, cudaStream_t s);
+
+} // namespace th

@@ -1,0 +1,59 @@
+// Host-side declarations shared by the CUDA translation units of the library.
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/torchhull_gb300.h"
+
+namespace th
+{
+
+struct CudaError
+{
+    cudaError_t code;
+    std::string where;
+};
+
+#define TH_CUDA(expr)                                                                                                  \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        cudaError_t th_err_ = (expr);                                                                                  \
+        if (th_err_ != cudaSuccess)                                                                                    \
+            throw ::th::CudaError{ th_err_, std::string(#expr) + " at " + __FILE__ + ":" + std::to_string(__LINE__) }; \
+    } while (0)
+
+#define TH_LAUNCH_CHECK() TH_CUDA(cudaGetLastError())
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+// Grid size for a grid-stride kernel over work_items items: enough blocks to
+// cover the work, at most 8 resident blocks per SM.
+int grid_for(int64_t work_items, int threads);
+
+// Integral image (sat.cu).  masks [B,H,W] of dtype, out [B,H,W] float32.
+void launch_integral_image(const void* masks, int dtype, int64_t B, int64_t H, int64_t W, float* out, cudaStream_t s);
+
+// Transform conversion to float32 row-major [B,16] (sat.cu).
+void launch_convert_transforms(const void* tf, int dtype, int64_t B, float* out, cudaStream_t s);
+
+// Gaussian blur (blur.cu).  edge_tiles: scratch of tiles_bytes(B,H,W,k) bytes.
+int64_t blur_tile_bytes(int64_t B, int64_t H, int64_t W, int kernel_size);
+void launch_gaussian_blur(const void* images,
+                          int idt,
+                          int64_t B,
+                          int64_t H,
+                          int64_t W,
+                          int kernel_size,
+                          float sigma,
+                          bool sparse,
+                          void* out,
+                          int odt,
+                          uint8_t* edge_tiles,
+                          cudaStream_t s);
+
+} // namespace th

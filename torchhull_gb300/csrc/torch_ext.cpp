@@ -1,0 +1,304 @@
+// Thin torch extension over the C ABI (include/torchhull_gb300.h).
+//
+// It keeps torchhull's Python-facing signatures, argument names, defaults and
+// error behaviour (src/torchhull/_C/python/bindings.cpp:12-251,
+// src/torchhull/_C/src/visual_hull.cpp:60-187, gaussian_blur.cpp:15-28):
+// tensors in, tensors out, RuntimeError on a failed check.  All computation
+// happens in libtorchhull_gb300.so on the current CUDA stream; outputs are
+// allocated here through torch's caching allocator once their sizes are known.
+
+#include <torch/extension.h>
+
+#include <ATen/cuda/CUDAContext.h>
+#include <c10/cuda/CUDAGuard.h>
+
+#include <array>
+#include <map>
+#include <mutex>
+#include <optional>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/torchhull_gb300.h"
+
+namespace
+{
+
+struct DeviceContext
+{
+    th_context* ctx = nullptr;
+    std::mutex lock;
+};
+
+DeviceContext& context_for(int device)
+{
+    static std::mutex registry_lock;
+    static std::map<int, DeviceContext*> registry;
+    std::lock_guard<std::mutex> g(registry_lock);
+    auto it = registry.find(device);
+    if (it != registry.end())
+        return *it->second;
+    auto* dc = new DeviceContext;
+    const th_status st = th_context_create(device, &dc->ctx);
+    TORCH_CHECK(st == TH_OK, "torchhull_gb300: cannot create a context on device ", device, ": ", th_status_string(st));
+    registry[device] = dc;
+    return *dc;
+}
+
+void check(th_status st, th_context* ctx)
+{
+    if (st == TH_OK)
+        return;
+    const std::string msg = th_context_error(ctx);
+    TORCH_CHECK(false, msg.empty() ? std::string(th_status_string(st)) : msg);
+}
+
+int32_t th_dtype_of(at::ScalarType t)
+{
+    switch (t)
+    {
+    case at::kBool:
+        return TH_BOOL;
+    case at::kByte:
+        return TH_UINT8;
+    case at::kChar:
+        return TH_INT8;
+    case at::kShort:
+        return TH_INT16;
+    case at::kInt:
+        return TH_INT32;
+    case at::kLong:
+        return TH_INT64;
+    case at::kHalf:
+        return TH_FLOAT16;
+    case at::kFloat:
+        return TH_FLOAT32;
+    case at::kDouble:
+        return TH_FLOAT64;
+    case at::kBFloat16:
+        return TH_BFLOAT16;
+    default:
+        return -1;
+    }
+}
+
+void* stream_of(const at::Tensor& t)
+{
+    return static_cast<void*>(at::cuda::getCurrentCUDAStream(t.device().index()).stream());
+}
+
+void require_cuda(const at::Tensor& t)
+{
+    TORCH_CHECK(t.is_cuda(), "No backend implementation available for device \"" + t.device().str() + "\".");
+}
+
+th_hull_args hull_args(const at::Tensor& masks,
+                       const at::Tensor& transforms,
+                       int level,
+                       const std::array<float, 3>& cube_corner_bfl,
+                       float cube_length,
+                       bool masks_partial,
+                       const std::string& transforms_convention,
+                       bool unique_verts)
+{
+    // visual_hull_cuda.cu:591-613
+    TORCH_CHECK_EQ(masks.device(), transforms.device());
+    TORCH_CHECK_EQ(masks.dim(), 4);
+    TORCH_CHECK_EQ(transforms.dim(), 3);
+    TORCH_CHECK_EQ(transforms.size(1), 4);
+    TORCH_CHECK_EQ(transforms.size(2), 4);
+    TORCH_CHECK_EQ(masks.size(0), transforms.size(0));
+    TORCH_CHECK_EQ(masks.size(3), 1);
+    TORCH_CHECK_GE(level, 0);
+    TORCH_CHECK_GT(cube_length, 0.f);
+    bool opengl = false;
+    if (transforms_convention == "opengl")
+        opengl = true;
+    else if (transforms_convention == "opencv")
+        opengl = false;
+    else
+        TORCH_CHECK(false, "Unsupported transforms_convention \"" + transforms_convention + "\".");
+
+    th_hull_args a{};
+    a.masks = masks.data_ptr();
+    a.masks_dtype = th_dtype_of(masks.scalar_type());
+    a.batch = masks.size(0);
+    a.height = masks.size(1);
+    a.width = masks.size(2);
+    a.transforms = transforms.data_ptr();
+    a.transforms_dtype = th_dtype_of(transforms.scalar_type());
+    a.level = level;
+    a.cube_corner_bfl[0] = cube_corner_bfl[0];
+    a.cube_corner_bfl[1] = cube_corner_bfl[1];
+    a.cube_corner_bfl[2] = cube_corner_bfl[2];
+    a.cube_length = cube_length;
+    a.masks_partial = masks_partial ? 1 : 0;
+    a.transforms_opengl = opengl ? 1 : 0;
+    a.unique_verts = unique_verts ? 1 : 0;
+    return a;
+}
+
+struct HullOutputs
+{
+    at::Tensor verts, faces;
+    std::vector<at::Tensor> candidates;
+    at::Tensor field_indices, field_values;
+};
+
+HullOutputs run_visual_hull(const at::Tensor& masks_in,
+                            const at::Tensor& transforms_in,
+                            int level,
+                            const std::array<float, 3>& cube_corner_bfl,
+                            float cube_length,
+                            bool masks_partial,
+                            const std::string& transforms_convention,
+                            bool unique_verts,
+                            bool want_candidates,
+                            bool want_field)
+{
+    require_cuda(masks_in);
+    at::cuda::CUDAGuard guard(masks_in.device());
+    const at::Tensor masks = masks_in.contiguous();
+    const at::Tensor transforms = transforms_in.contiguous();
+    th_hull_args a = hull_args(masks, transforms, level, cube_corner_bfl, cube_length, masks_partial,
+                               transforms_convention, unique_verts);
+
+    DeviceContext& dc = context_for(masks.device().index());
+    std::lock_guard<std::mutex> g(dc.lock);
+    void* stream = stream_of(masks);
+    th_hull_info info{};
+    check(th_visual_hull(dc.ctx, &a, stream, &info), dc.ctx);
+
+    const auto dev = masks.device();
+    HullOutputs out;
+    out.verts = at::empty({ info.num_verts, 3 }, at::TensorOptions().dtype(at::kFloat).device(dev));
+    out.faces = at::empty({ info.num_faces, 3 }, at::TensorOptions().dtype(at::kLong).device(dev));
+    check(th_visual_hull_export(dc.ctx, out.verts.data_ptr<float>(), out.faces.data_ptr<int64_t>(), stream), dc.ctx);
+    if (want_candidates)
+    {
+        for (int i = 0; i < info.num_levels; ++i)
+        {
+            at::Tensor c = at::empty({ info.level_sizes[i] }, at::TensorOptions().dtype(at::kLong).device(dev));
+            check(th_visual_hull_export_candidates(dc.ctx, i, c.data_ptr<int64_t>(), stream), dc.ctx);
+            out.candidates.push_back(c);
+        }
+    }
+    if (want_field)
+    {
+        out.field_indices = at::empty({ info.num_corners }, at::TensorOptions().dtype(at::kLong).device(dev));
+        out.field_values = at::empty({ info.num_corners }, at::TensorOptions().dtype(at::kFloat).device(dev));
+        check(th_visual_hull_export_field(dc.ctx, out.field_indices.data_ptr<int64_t>(),
+                                          out.field_values.data_ptr<float>(), stream),
+              dc.ctx);
+    }
+    return out;
+}
+
+std::tuple<at::Tensor, at::Tensor> visual_hull(const at::Tensor& masks,
+                                               const at::Tensor& transforms,
+                                               int level,
+                                               const std::array<float, 3>& cube_corner_bfl,
+                                               float cube_length,
+                                               bool masks_partial,
+                                               const std::string& transforms_convention,
+                                               bool unique_verts)
+{
+    auto o = run_visual_hull(masks, transforms, level, cube_corner_bfl, cube_length, masks_partial,
+                             transforms_convention, unique_verts, false, false);
+    return { o.verts, o.faces };
+}
+
+std::tuple<at::Tensor, at::Tensor, std::vector<at::Tensor>> visual_hull_with_candidate_voxels(
+        const at::Tensor& masks,
+        const at::Tensor& transforms,
+        int level,
+        const std::array<float, 3>& cube_corner_bfl,
+        float cube_length,
+        bool masks_partial,
+        const std::string& transforms_convention,
+        bool unique_verts)
+{
+    auto o = run_visual_hull(masks, transforms, level, cube_corner_bfl, cube_length, masks_partial,
+                             transforms_convention, unique_verts, true, false);
+    return { o.verts, o.faces, o.candidates };
+}
+
+// The sparse field as (indices, values, grid size R); the Python layer turns
+// it into torchhull's coalesced COO tensor (visual_hull_cuda.cu:522-580).
+std::tuple<at::Tensor, at::Tensor, int64_t> sparse_visual_hull_field_raw(const at::Tensor& masks,
+                                                                         const at::Tensor& transforms,
+                                                                         int level,
+                                                                         const std::array<float, 3>& cube_corner_bfl,
+                                                                         float cube_length,
+                                                                         bool masks_partial,
+                                                                         const std::string& transforms_convention)
+{
+    auto o = run_visual_hull(masks, transforms, level, cube_corner_bfl, cube_length, masks_partial,
+                             transforms_convention, true, false, true);
+    return { o.field_indices, o.field_values, (int64_t{ 1 } << level) + 1 };
+}
+
+at::Tensor gaussian_blur(const at::Tensor& images_in,
+                         int kernel_size,
+                         float sigma,
+                         bool sparse,
+                         std::optional<at::ScalarType> dtype)
+{
+    require_cuda(images_in);
+    at::cuda::CUDAGuard guard(images_in.device());
+    TORCH_CHECK_EQ(images_in.dim(), 4);
+    TORCH_CHECK_EQ(images_in.size(3), 1);
+    const at::Tensor images = images_in.contiguous();
+    const at::ScalarType out_type = dtype.value_or(images.scalar_type());
+    at::Tensor out = at::empty(images.sizes(), images.options().dtype(out_type));
+    DeviceContext& dc = context_for(images.device().index());
+    std::lock_guard<std::mutex> g(dc.lock);
+    check(th_gaussian_blur(dc.ctx, images.data_ptr(), th_dtype_of(images.scalar_type()), images.size(0),
+                           images.size(1), images.size(2), kernel_size, sigma, sparse ? 1 : 0, out.data_ptr(),
+                           th_dtype_of(out_type), stream_of(images)),
+          dc.ctx);
+    return out;
+}
+
+at::Tensor integral_image(const at::Tensor& masks_in)
+{
+    require_cuda(masks_in);
+    at::cuda::CUDAGuard guard(masks_in.device());
+    TORCH_CHECK_EQ(masks_in.dim(), 4);
+    const at::Tensor masks = masks_in.contiguous();
+    at::Tensor out = at::empty({ masks.size(0), masks.size(1), masks.size(2) }, masks.options().dtype(at::kFloat));
+    DeviceContext& dc = context_for(masks.device().index());
+    std::lock_guard<std::mutex> g(dc.lock);
+    check(th_integral_image(dc.ctx, masks.data_ptr(), th_dtype_of(masks.scalar_type()), masks.size(0), masks.size(1),
+                            masks.size(2) * masks.size(3), out.data_ptr<float>(), stream_of(masks)),
+          dc.ctx);
+    return out;
+}
+
+int64_t device_pool_bytes(int device)
+{
+    DeviceContext& dc = context_for(device);
+    std::lock_guard<std::mutex> g(dc.lock);
+    return th_context_device_bytes(dc.ctx);
+}
+
+} // namespace
+
+PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
+{
+    using namespace pybind11::literals;
+    m.def("visual_hull", &visual_hull, "masks"_a, "transforms"_a, "level"_a, "cube_corner_bfl"_a, "cube_length"_a,
+          "masks_partial"_a, "transforms_convention"_a, "unique_verts"_a = true,
+          "Visual hull of the masks as a mesh (verts [V,3] float32, faces [F,3] int64).");
+    m.def("visual_hull_with_candidate_voxels", &visual_hull_with_candidate_voxels, "masks"_a, "transforms"_a, "level"_a,
+          "cube_corner_bfl"_a, "cube_length"_a, "masks_partial"_a, "transforms_convention"_a, "unique_verts"_a = true,
+          "visual_hull plus the ravelled candidate cells of every octree level.");
+    m.def("sparse_visual_hull_field_raw", &sparse_visual_hull_field_raw, "masks"_a, "transforms"_a, "level"_a,
+          "cube_corner_bfl"_a, "cube_length"_a, "masks_partial"_a, "transforms_convention"_a,
+          "Sparse hull field as (ravelled indices, values, grid size).");
+    m.def("gaussian_blur", &gaussian_blur, "images"_a, "kernel_size"_a, "sigma"_a, "sparse"_a = true,
+          "dtype"_a = pybind11::none(), "Gaussian blur of [B,H,W,1] images.");
+    m.def("integral_image", &integral_image, "masks"_a, "Float32 integral image [B,H,W] of masks [B,H,W,1].");
+    m.def("device_pool_bytes", &device_pool_bytes, "device"_a, "Bytes held by the device's resident pools.");
+}
