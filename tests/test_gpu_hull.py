@@ -115,6 +115,10 @@ def test_integral_image_bitwise(th, cuda, dtype):
     sat = th.integral_image(masks.to(cuda)).cpu().numpy()
     ref = oracle.integral_image(masks)
     assert np.array_equal(sat.view(np.uint32), ref.view(np.uint32))
+    # the reference's own construction, torch.cumsum on the device (visual_hull_cuda.cu:76-90)
+    m = masks.to(cuda)
+    ref_torch = torch.cumsum(torch.cumsum(m, 1, dtype=torch.float32), 2, dtype=torch.float32)[..., 0].cpu().numpy()
+    assert np.array_equal(sat.view(np.uint32), ref_torch.view(np.uint32))
 
 
 def test_arithmetic_probe(cuda):
