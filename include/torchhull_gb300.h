@@ -161,6 +161,27 @@ th_status th_integral_image(th_context* ctx,
 th_status th_visual_hull_batch(th_context* ctx, const th_hull_args* args, int32_t n, void* stream, th_hull_info* infos);
 th_status th_visual_hull_batch_export(th_context* ctx, int32_t index, float* verts, int64_t* faces, void* stream);
 
+/* Stage timing (no reference counterpart).  With profiling on, th_visual_hull
+ * records CUDA events between its stages on the request's stream; the times
+ * of the last request, in milliseconds, are read back with
+ * th_context_stage_times.  Off by default (no events recorded). */
+typedef struct th_stage_times
+{
+    float integral_image_ms; /* transforms conversion + SAT */
+    float carve_ms[TH_MAX_LEVEL]; /* classify + compact, per parent level */
+    float corners_ms;             /* corner bitmap, row scan, corner ranks */
+    float field_ms;
+    float marching_cubes_ms; /* cell codes, edge marks, vertex numbering */
+    float total_ms;
+    int32_t levels;
+} th_stage_times;
+
+th_status th_context_set_profiling(th_context* ctx, int32_t enable);
+th_status th_context_stage_times(const th_context* ctx, th_stage_times* out);
+
+/* Number of kernels this library has launched in this process (all contexts). */
+int64_t th_launch_count(void);
+
 /* Diagnostics (no reference counterpart): evaluates the device arithmetic the
  * oracle emulates: out_i64[i] = (int64) in[i] as the GPU converts it, and
  * out_f32[i] = c + v[i]/r * L written as the reference writes it. */

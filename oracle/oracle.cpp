@@ -91,11 +91,12 @@ bool is_float_dtype(int d)
 // ---------------------------------------------------------------------------
 // device arithmetic rules
 
-// float -> int64 the way the GPU converts (cvt.rzi.s64.f32): NaN -> 0, saturate.
+// float -> int64 the way the GPU converts (cvt.rzi.s64.f32): saturate, and
+// NaN -> INT64_MIN (measured on GB300 by the arithmetic probe test).
 int64_t f2i64(float f)
 {
     if (std::isnan(f))
-        return 0;
+        return std::numeric_limits<int64_t>::min();
     if (f >= 9223372036854775808.0f)
         return std::numeric_limits<int64_t>::max();
     if (f <= -9223372036854775808.0f)

@@ -9,6 +9,7 @@
 // request runs again, so repeated requests of similar size never allocate.
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -19,6 +20,23 @@
 
 namespace th
 {
+
+namespace
+{
+std::atomic<int64_t> g_launches{ 0 };
+}
+
+void note_launches(int n)
+{
+    g_launches.fetch_add(n, std::memory_order_relaxed);
+}
+
+void check_launch(const char* what)
+{
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        throw CudaError{ e, std::string("kernel launch: ") + what };
+}
 
 int sm_count()
 {
@@ -120,6 +138,49 @@ struct HullSlot
 } // namespace
 } // namespace th
 
+namespace th
+{
+namespace
+{
+
+// CUDA events between the stages of one request (th_context_set_profiling).
+struct StageEvents
+{
+    static constexpr int kCount = TH_MAX_LEVEL + 6;
+    cudaEvent_t ev[kCount] = {};
+    bool ready = false;
+
+    void create()
+    {
+        if (ready)
+            return;
+        for (auto& e : ev)
+            TH_CUDA(cudaEventCreate(&e));
+        ready = true;
+    }
+    void destroy()
+    {
+        if (!ready)
+            return;
+        for (auto& e : ev)
+            cudaEventDestroy(e);
+        ready = false;
+    }
+    void record(int i, cudaStream_t s)
+    {
+        TH_CUDA(cudaEventRecord(ev[i], s));
+    }
+    float between(int a, int b) const
+    {
+        float ms = 0.f;
+        TH_CUDA(cudaEventElapsedTime(&ms, ev[a], ev[b]));
+        return ms;
+    }
+};
+
+} // namespace
+} // namespace th
+
 struct th_context
 {
     int device = 0;
@@ -127,6 +188,9 @@ struct th_context
     th::HullSlot hull;
     std::vector<th::HullSlot> batch;
     th::DevBuf blur_scratch;
+    bool profiling = false;
+    th::StageEvents events;
+    th_stage_times times{};
 };
 
 namespace th
@@ -303,7 +367,7 @@ void fill_info(const HullSlot& s, th_hull_info* info)
     *info = out;
 }
 
-void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t st)
+void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t st, StageEvents* ev)
 {
     validate(a);
     if (s.dirty)
@@ -313,21 +377,38 @@ void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t 
         s.dirty = false;
     }
     s.has_result = false;
+    const int L = a->level;
     for (int attempt = 0; attempt < 8; ++attempt)
     {
         prepare(s, a, st);
         const HullPlan& p = s.plan;
         if (attempt == 0)
         {
+            if (ev)
+                ev->record(0, st);
             launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), st);
             launch_integral_image(a->masks, a->masks_dtype, a->batch, a->height, a->width, s.sat.as<float>(), st);
+            if (ev)
+                ev->record(1, st);
         }
         launch_hull_init(p, st);
         for (int li = 0; li < p.level; ++li)
+        {
             launch_carve_level(p, li, st);
+            if (ev)
+                ev->record(2 + li, st);
+        }
+        if (ev)
+            ev->record(L + 2, st);
         launch_corners(p, st);
+        if (ev)
+            ev->record(L + 3, st);
         launch_field(p, st);
+        if (ev)
+            ev->record(L + 4, st);
         launch_marching_cubes(p, st);
+        if (ev)
+            ev->record(L + 5, st);
         TH_CUDA(cudaMemcpyAsync(s.host, p.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
         TH_CUDA(cudaStreamSynchronize(st));
         s.dirty = true;
@@ -345,7 +426,19 @@ void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t 
     }
     fill_info(s, &s.info);
     s.has_result = true;
-    (void)ctx;
+    if (ev)
+    {
+        th_stage_times t{};
+        t.levels = L;
+        t.integral_image_ms = ev->between(0, 1);
+        for (int li = 0; li < L; ++li)
+            t.carve_ms[li] = ev->between(1 + li, 2 + li);
+        t.corners_ms = ev->between(L + 2, L + 3);
+        t.field_ms = ev->between(L + 3, L + 4);
+        t.marching_cubes_ms = ev->between(L + 4, L + 5);
+        t.total_ms = ev->between(0, L + 5);
+        ctx->times = t;
+    }
 }
 
 th_status fail(th_context* ctx, th_status st, const std::string& msg)
@@ -417,6 +510,7 @@ void th_context_destroy(th_context* ctx)
     for (auto& s : ctx->batch)
         s.release();
     ctx->blur_scratch.release();
+    ctx->events.destroy();
     cudaSetDevice(prev);
     delete ctx;
 }
@@ -453,10 +547,32 @@ int64_t th_context_device_bytes(const th_context* ctx)
     return ctx ? pool_bytes(ctx) : 0;
 }
 
+th_status th_context_set_profiling(th_context* ctx, int32_t enable)
+{
+    return guarded(ctx, [&] {
+        if (enable)
+            ctx->events.create();
+        ctx->profiling = enable != 0;
+    });
+}
+
+th_status th_context_stage_times(const th_context* ctx, th_stage_times* out)
+{
+    if (!ctx || !out)
+        return TH_ERR_INVALID_ARGUMENT;
+    *out = ctx->times;
+    return TH_OK;
+}
+
+int64_t th_launch_count(void)
+{
+    return g_launches.load(std::memory_order_relaxed);
+}
+
 th_status th_visual_hull(th_context* ctx, const th_hull_args* args, void* stream, th_hull_info* info)
 {
     return guarded(ctx, [&] {
-        run_hull(ctx, ctx->hull, args, static_cast<cudaStream_t>(stream));
+        run_hull(ctx, ctx->hull, args, static_cast<cudaStream_t>(stream), ctx->profiling ? &ctx->events : nullptr);
         if (info)
             *info = ctx->hull.info;
     });
@@ -598,7 +714,7 @@ th_status th_visual_hull_batch(th_context* ctx, const th_hull_args* args, int32_
         auto st = static_cast<cudaStream_t>(stream);
         for (int32_t i = 0; i < n; ++i)
         {
-            run_hull(ctx, ctx->batch[i], &args[i], st);
+            run_hull(ctx, ctx->batch[i], &args[i], st, nullptr);
             infos[i] = ctx->batch[i].info;
         }
     });

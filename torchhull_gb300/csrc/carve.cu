@@ -268,7 +268,6 @@ void launch_carve_level(const HullPlan& p, int li, cudaStream_t s)
     TH_LAUNCH_CHECK();
     run_scan(ChildCount{ p.child_masks }, ChildEmit{ p, li }, ChildEpilogue{ p.ctr, li, p.node_cap },
              Count{ &p.ctr->level_count[li], 0 }, max_parents, p.tile_sums, &p.ctr->scan, s);
-    TH_LAUNCH_CHECK();
 }
 
 } // namespace th

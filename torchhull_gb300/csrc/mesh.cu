@@ -498,10 +498,8 @@ void launch_corners(const HullPlan& p, cudaStream_t s)
     const int64_t row_words = (p.R * p.R + 31) / 32;
     run_scan(RowCount{ p.rowbits }, RowEmit{ p.rowbits, p.rows }, RowEpilogue{ p.ctr }, Count{ nullptr, row_words },
              row_words, p.tile_sums, &p.ctr->scan, s);
-    TH_LAUNCH_CHECK();
     run_scan(CornerCount{ p }, CornerEmit{ p }, CornerEpilogue{ p.ctr, p.corner_cap }, Count{ &p.ctr->rows, 0 },
              p.R * p.R, p.tile_sums, &p.ctr->scan, s);
-    TH_LAUNCH_CHECK();
 }
 
 void launch_field(const HullPlan& p, cudaStream_t s)
@@ -524,7 +522,6 @@ void launch_marching_cubes(const HullPlan& p, cudaStream_t s)
     TH_LAUNCH_CHECK();
     run_scan(VertCount{ p.codes, p.emask }, VertEmit{ p.soup_off, p.vbase }, VertEpilogue{ p.ctr },
              Count{ &p.ctr->corners, 0 }, p.corner_cap, p.tile_sums, &p.ctr->scan, s);
-    TH_LAUNCH_CHECK();
 }
 
 void launch_export(const HullPlan& p, float* verts, int64_t* faces, cudaStream_t s)

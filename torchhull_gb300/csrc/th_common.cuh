@@ -325,6 +325,8 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(CountF count,
 }
 
 int sm_count();
+void note_launches(int n);
+void check_launch(const char* what);
 
 // Both scan passes on stream s.  n_max bounds the item count on the host side
 // (it sizes the grid; tile_sums must hold ceil(n_max / kScanTile) entries).
@@ -343,6 +345,8 @@ inline void run_scan(CountF count,
     const int grid = static_cast<int>(tiles < 1 ? 1 : (tiles < cap ? tiles : cap));
     scan_reduce_kernel<<<grid, kScanThreads, 0, s>>>(count, n, tile_sums, state, epi);
     scan_apply_kernel<<<grid, kScanThreads, 0, s>>>(count, emit, n, tile_sums);
+    check_launch("device-wide scan");
+    note_launches(2);
 }
 
 } // namespace th

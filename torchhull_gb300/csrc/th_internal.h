@@ -26,7 +26,18 @@ struct CudaError
             throw ::th::CudaError{ th_err_, std::string(#expr) + " at " + __FILE__ + ":" + std::to_string(__LINE__) }; \
     } while (0)
 
-#define TH_LAUNCH_CHECK() TH_CUDA(cudaGetLastError())
+// Counts kernels launched by this library (th_launch_count).
+void note_launches(int n);
+// Throws CudaError if the last launch failed.
+void check_launch(const char* what);
+
+// After one kernel launch: check it and count it.
+#define TH_LAUNCH_CHECK()                                                                                              \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        TH_CUDA(cudaGetLastError());                                                                                   \
+        ::th::note_launches(1);                                                                                        \
+    } while (0)
 
 // Number of SMs of the current device (cached per device).
 int sm_count();

@@ -283,6 +283,38 @@ int64_t device_pool_bytes(int device)
     return th_context_device_bytes(dc.ctx);
 }
 
+void set_profiling(int device, bool enable)
+{
+    DeviceContext& dc = context_for(device);
+    std::lock_guard<std::mutex> g(dc.lock);
+    check(th_context_set_profiling(dc.ctx, enable ? 1 : 0), dc.ctx);
+}
+
+// Stage times (ms) of the device's last visual_hull call made with profiling on.
+pybind11::dict stage_times(int device)
+{
+    DeviceContext& dc = context_for(device);
+    std::lock_guard<std::mutex> g(dc.lock);
+    th_stage_times t{};
+    check(th_context_stage_times(dc.ctx, &t), dc.ctx);
+    pybind11::dict d;
+    d["integral_image"] = t.integral_image_ms;
+    pybind11::list carve;
+    for (int i = 0; i < t.levels; ++i)
+        carve.append(t.carve_ms[i]);
+    d["carve"] = carve;
+    d["corners"] = t.corners_ms;
+    d["field"] = t.field_ms;
+    d["marching_cubes"] = t.marching_cubes_ms;
+    d["total"] = t.total_ms;
+    return d;
+}
+
+int64_t launch_count()
+{
+    return th_launch_count();
+}
+
 } // namespace
 
 PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
@@ -301,4 +333,7 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
           "dtype"_a = pybind11::none(), "Gaussian blur of [B,H,W,1] images.");
     m.def("integral_image", &integral_image, "masks"_a, "Float32 integral image [B,H,W] of masks [B,H,W,1].");
     m.def("device_pool_bytes", &device_pool_bytes, "device"_a, "Bytes held by the device's resident pools.");
+    m.def("set_profiling", &set_profiling, "device"_a, "enable"_a, "Record CUDA events between hull stages.");
+    m.def("stage_times", &stage_times, "device"_a, "Stage times (ms) of the last profiled visual_hull call.");
+    m.def("launch_count", &launch_count, "Kernels launched by the CUDA library in this process.");
 }
