@@ -139,6 +139,31 @@ th_status th_gaussian_blur(th_context* ctx,
                            int32_t out_dtype,
                            void* stream);
 
+/*
+ * th_gaussian_blur without any device allocation, for callers that cannot
+ * call cudaMalloc: a process whose device memory another framework has already
+ * reserved, a per-frame loop that must not risk the device-wide synchronisation
+ * cudaMalloc/cudaFree can cause, or a caller with a fixed device-memory budget.
+ * No counterpart in the reference.  Same arguments and results as
+ * th_gaussian_blur, but no context: its scratch is one 16 MiB array in the
+ * library's device memory, held on every GPU that loads the library.  Requests
+ * whose tile flags and weights (B*(H/(k/2)+1)*(W/(k/2)+1) + 8*(k*k+1) + 16
+ * bytes) exceed 16 MiB return TH_ERR_INVALID_ARGUMENT.  All calls share that
+ * array, so calls whose work overlaps on the GPU race.  The first call on a
+ * device looks up the array's device address; make it before any stream capture.
+ */
+th_status th_gaussian_blur_noalloc(const void* images,
+                                   int32_t images_dtype,
+                                   int64_t batch,
+                                   int64_t height,
+                                   int64_t width,
+                                   int32_t kernel_size,
+                                   float sigma,
+                                   int32_t sparse,
+                                   void* out,
+                                   int32_t out_dtype,
+                                   void* stream);
+
 /* The float32 integral image of masks [B,H,W,1] into out [B,H,W], with the
  * exact rounding of torch::cumsum(dim 1) then (dim 2) that the reference uses
  * (visual_hull_cuda.cu:76-90). */
