@@ -5,8 +5,8 @@
 // small counter block at the end (the reference synchronises after every
 // kernel and reads counts back per level, visual_hull_cuda.cu:742, :820 and
 // marching_cubes_cuda.cu:600-634).  Pools only grow: a request whose octree or
-// corner set outgrows them is detected on the device, the pools double and the
-// request runs again, so repeated requests of similar size never allocate.
+// corner set outgrows them is detected on the device, the pools grow fourfold
+// and the request runs again, so repeated requests of similar size never allocate.
 
 #include <algorithm>
 #include <atomic>
@@ -244,6 +244,8 @@ void validate(const th_hull_args* a)
     // Flagged/Unique/stdgpu use 32-bit indices (visual_hull_cuda.cu:716, :798)
     if (a->batch * a->height * a->width >= (int64_t{ 1 } << 40))
         throw ArgError{ TH_ERR_INVALID_ARGUMENT, "masks too large" };
+    if (a->height >= (int64_t{ 1 } << 31) || a->width >= (int64_t{ 1 } << 31))
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "mask height and width must be below 2^31" };
 }
 
 int64_t max_nodes(int level)
@@ -264,8 +266,10 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st)
     const int64_t WR = (R + 63) / 64;
     if (s.node_cap == 0)
     {
-        s.node_cap = std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 22);
-        s.corner_cap = std::min<int64_t>(R * R * R, int64_t{ 1 } << 23);
+        // 16 M nodes and corners (about 0.5 GB) cover a level-9 hull of 32
+        // megapixel views without a rerun; the pools grow x4 beyond that.
+        s.node_cap = std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 24);
+        s.corner_cap = std::min<int64_t>(R * R * R, int64_t{ 1 } << 24);
     }
     s.node_cap = std::max<int64_t>(s.node_cap, std::min<int64_t>(max_nodes(L), 4096));
     s.corner_cap = std::max<int64_t>(s.corner_cap, std::min<int64_t>(R * R * R, 4096));
@@ -392,9 +396,14 @@ void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t 
                 ev->record(1, st);
         }
         launch_hull_init(p, st);
+        // With an empty image every child is empty in the first view (the
+        // reference samples zeros everywhere), so the octree stops at the root;
+        // without views nothing is refined either.  Skip the carve in both cases.
+        const bool carve = p.B > 0 && p.H > 0 && p.W > 0;
         for (int li = 0; li < p.level; ++li)
         {
-            launch_carve_level(p, li, st);
+            if (carve)
+                launch_carve_level(p, li, st);
             if (ev)
                 ev->record(2 + li, st);
         }
@@ -418,9 +427,9 @@ void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t 
         launch_cleanup(p, st);
         s.dirty = false;
         if (ovf & kOverflowNodes)
-            s.node_cap *= 2;
+            s.node_cap *= 4;
         if (ovf & kOverflowCorners)
-            s.corner_cap *= 2;
+            s.corner_cap *= 4;
         if (attempt == 7)
             throw ArgError{ TH_ERR_OUT_OF_MEMORY, "visual hull pools could not be grown enough" };
     }

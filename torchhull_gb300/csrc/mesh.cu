@@ -199,16 +199,46 @@ struct CornerEpilogue
 template <int DT>
 __device__ __forceinline__ float mask_sample(const HullPlan& p, int64_t b, int64_t y, int64_t x, float pad)
 {
-    return in_image(y, x, p.H, p.W) ? load_f32<DT>(p.masks, (b * p.H + y) * p.W + x) : pad;
+    return (0 <= y && y < p.H && 0 <= x && x < p.W) ? load_f32<DT>(p.masks, (b * p.H + y) * p.W + x) : pad;
 }
 
-__device__ __forceinline__ int64_t add1(int64_t v)
+// Factor of view b for the corner at world point (wx, wy, wz): the bilinear
+// mask sample (image_utils.h:162-214), or exactly 1 when partial mode skips
+// the view (x * 1 == x, so multiplying by it equals skipping it).
+//
+// The reference converts the rounded pixel to int64.  This uses the
+// saturating int32 conversion (64-bit conversions run on GB300's FP64 pipe):
+// the in-image tests decide identically, and where the two values differ
+// (|coordinate| >= 2^31) all four samples are padding, for which the
+// interpolation gives the same result (0, 1 or NaN) for either weight.
+template <int DT, bool PARTIAL>
+__device__ __forceinline__ float view_factor(const HullPlan& p, int64_t b, float wx, float wy, float wz, float Hf, float Wf)
 {
-    return static_cast<int64_t>(static_cast<uint64_t>(v) + 1u);
+    const float* m = p.tf + 16 * b;
+    float px, py;
+    to_pixel(m, wx, wy, wz, p.opengl, Hf, Wf, px, py);
+    const float pad = PARTIAL ? 1.f : 0.f;
+    if (PARTIAL)
+    {
+        const int64_t qx = __float2int_rz(roundf(px)), qy = __float2int_rz(roundf(py));
+        if (!(1 <= qy && qy < p.H - 1 && 1 <= qx && qx < p.W - 1))
+            return 1.f;
+    }
+    const int32_t yp = __float2int_rz(roundf(__fadd_rn(py, -0.5f)));
+    const int32_t xp = __float2int_rz(roundf(__fadd_rn(px, -0.5f)));
+    const int64_t y0 = yp, x0 = xp;
+    const float v00 = mask_sample<DT>(p, b, y0, x0, pad);
+    const float v10 = mask_sample<DT>(p, b, y0 + 1, x0, pad);
+    const float v01 = mask_sample<DT>(p, b, y0, x0 + 1, pad);
+    const float v11 = mask_sample<DT>(p, b, y0 + 1, x0 + 1, pad);
+    const float ty = __fsub_rn(py, __int2float_rn(yp));
+    const float tx = __fsub_rn(px, __int2float_rn(xp));
+    return bilerp(v00, v10, v01, v11, ty, tx);
 }
 
-// accumulate_hull_counts_{full,partial} (visual_hull_cuda.cu:419-520) and the
-// bilinear samplers (image_utils.h:162-214), all views in one thread.
+// accumulate_hull_counts_{full,partial} (visual_hull_cuda.cu:419-520): all
+// views in one thread, multiplied in ascending view order; the factors of
+// consecutive views are independent, so their loads overlap.
 template <int DT, bool PARTIAL>
 __global__ void __launch_bounds__(256) field_kernel(HullPlan p)
 {
@@ -216,7 +246,6 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p)
     const int64_t R = p.R;
     const float rcf = static_cast<float>(R - 1);
     const float Hf = static_cast<float>(p.H), Wf = static_cast<float>(p.W);
-    const float pad = PARTIAL ? 1.f : 0.f;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
     {
@@ -226,27 +255,9 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p)
         const float wy = world_coordinate(gy, rcf, p.corner[1], p.length);
         const float wz = world_coordinate(gz, rcf, p.corner[2], p.length);
         float value = 1.f;
+#pragma unroll 4
         for (int64_t b = 0; b < p.B; ++b)
-        {
-            const float* m = p.tf + 16 * b;
-            float px, py;
-            to_pixel(m, wx, wy, wz, p.opengl, Hf, Wf, px, py);
-            if (PARTIAL)
-            {
-                const int64_t rx = f2i64(roundf(px)), ry = f2i64(roundf(py));
-                if (!in_image(ry, rx, p.H, p.W, 1))
-                    continue;
-            }
-            const int64_t yp = f2i64(roundf(__fadd_rn(py, -0.5f)));
-            const int64_t xp = f2i64(roundf(__fadd_rn(px, -0.5f)));
-            const float v00 = mask_sample<DT>(p, b, yp, xp, pad);
-            const float v10 = mask_sample<DT>(p, b, add1(yp), xp, pad);
-            const float v01 = mask_sample<DT>(p, b, yp, add1(xp), pad);
-            const float v11 = mask_sample<DT>(p, b, add1(yp), add1(xp), pad);
-            const float ty = __fsub_rn(py, __ll2float_rn(yp));
-            const float tx = __fsub_rn(px, __ll2float_rn(xp));
-            value = __fmul_rn(value, bilerp(v00, v10, v01, v11, ty, tx));
-        }
+            value = __fmul_rn(value, view_factor<DT, PARTIAL>(p, b, wx, wy, wz, Hf, Wf));
         p.values[t] = value;
     }
 }
