@@ -110,10 +110,9 @@ bool is_image_dtype(int d)
 // Pools and the state of the last request of one context.
 struct HullSlot
 {
-    DevBuf tf, sat, nodes, child_masks, tile_sums, bitmap, word_rank, rowbits, rows, corners, values, codes, emask,
-            soup_off, vbase, counters;
-    int64_t node_cap = 0, corner_cap = 0;
-    int64_t bitmap_words = 0, rowbit_words = 0;
+    DevBuf tf, sat, nodes, node_skip, child_masks, child_skip, tile_sums, bitmap, word_rank, rowbits, rows, corners,
+            corner_skip, values, codes, emask, soup_off, vbase, counters, flags;
+    int64_t node_cap = 0, corner_cap = 0, parent_cap = 0;
     HullPlan plan{};
     DevCounters* host = nullptr; // pinned copy of the counters
     th_hull_info info{};
@@ -121,11 +120,17 @@ struct HullSlot
     bool dirty = false; // bitmap rows of the last request still set
     cudaEvent_t done = nullptr;
 
+    std::vector<const DevBuf*> buffers() const
+    {
+        return { &tf,      &sat,  &nodes,     &node_skip,   &child_masks, &child_skip, &tile_sums,
+                 &bitmap,  &word_rank, &rowbits, &rows,   &corners,     &corner_skip, &values,
+                 &codes,   &emask, &soup_off,  &vbase,       &counters,    &flags };
+    }
+
     void release()
     {
-        for (DevBuf* b : { &tf, &sat, &nodes, &child_masks, &tile_sums, &bitmap, &word_rank, &rowbits, &rows, &corners,
-                           &values, &codes, &emask, &soup_off, &vbase, &counters })
-            b->release();
+        for (const DevBuf* b : buffers())
+            const_cast<DevBuf*>(b)->release();
         if (host)
             cudaFreeHost(host);
         host = nullptr;
@@ -202,9 +207,7 @@ int64_t pool_bytes(const th_context* ctx)
 {
     auto sum = [](const HullSlot& s) {
         int64_t b = 0;
-        for (const DevBuf* d : { &s.tf, &s.sat, &s.nodes, &s.child_masks, &s.tile_sums, &s.bitmap, &s.word_rank,
-                                 &s.rowbits, &s.rows, &s.corners, &s.values, &s.codes, &s.emask, &s.soup_off, &s.vbase,
-                                 &s.counters })
+        for (const DevBuf* d : s.buffers())
             b += static_cast<int64_t>(d->bytes);
         return b;
     };
@@ -270,16 +273,23 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st)
         // megapixel views without a rerun; the pools grow x4 beyond that.
         s.node_cap = std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 24);
         s.corner_cap = std::min<int64_t>(R * R * R, int64_t{ 1 } << 24);
+        s.parent_cap = std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 22);
     }
     s.node_cap = std::max<int64_t>(s.node_cap, std::min<int64_t>(max_nodes(L), 4096));
     s.corner_cap = std::max<int64_t>(s.corner_cap, std::min<int64_t>(R * R * R, 4096));
+    s.parent_cap = std::max<int64_t>(s.parent_cap, std::min<int64_t>(max_nodes(L), 4096));
     const int64_t node_cap = std::min<int64_t>(s.node_cap, max_nodes(L));
     const int64_t corner_cap = std::min<int64_t>(s.corner_cap, R * R * R);
+    const int64_t parent_cap = std::min<int64_t>(s.parent_cap, node_cap);
 
     s.tf.ensure(sizeof(float) * std::max<int64_t>(B, 1) * 16);
     s.sat.ensure(sizeof(float) * std::max<int64_t>(B * H * W, 1));
     s.nodes.ensure(sizeof(int64_t) * node_cap);
+    s.node_skip.ensure(sizeof(uint32_t) * node_cap);
     s.child_masks.ensure(node_cap);
+    s.child_skip.ensure(sizeof(uint32_t) * 8 * parent_cap);
+    s.corner_skip.ensure(sizeof(uint32_t) * corner_cap);
+    s.flags.ensure(sizeof(unsigned int) * 4);
     const int64_t scan_items = std::max({ node_cap, corner_cap, R * R });
     s.tile_sums.ensure(sizeof(unsigned long long) * ((scan_items + kScanTile - 1) / kScanTile + 1));
     const int64_t words = R * R * WR;
@@ -324,6 +334,13 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st)
     p.node_cap = node_cap;
     p.child_masks = s.child_masks.as<uint8_t>();
     p.tile_sums = s.tile_sums.as<unsigned long long>();
+    p.node_skip = s.node_skip.as<uint32_t>();
+    p.child_skip = s.child_skip.as<uint32_t>();
+    p.corner_skip = s.corner_skip.as<uint32_t>();
+    p.parent_cap = parent_cap;
+    p.nonbinary = s.flags.as<unsigned int>();
+    // exact integer box sums need every SAT sum of two entries below 2^24
+    p.skip_ok = B > 0 && H > 0 && W > 0 && H * W <= (int64_t{ 1 } << 23);
     p.R = R;
     p.WR = WR;
     p.bitmap = s.bitmap.as<uint64_t>();
@@ -391,7 +408,9 @@ void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t 
             if (ev)
                 ev->record(0, st);
             launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), st);
-            launch_integral_image(a->masks, a->masks_dtype, a->batch, a->height, a->width, s.sat.as<float>(), st);
+            TH_CUDA(cudaMemsetAsync(s.flags.p, 0, sizeof(unsigned int), st));
+            launch_integral_image(a->masks, a->masks_dtype, a->batch, a->height, a->width, s.sat.as<float>(), st,
+                                  s.flags.as<unsigned int>());
             if (ev)
                 ev->record(1, st);
         }
@@ -422,7 +441,12 @@ void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t 
         TH_CUDA(cudaStreamSynchronize(st));
         s.dirty = true;
         const int64_t ovf = s.host->overflow;
-        if (ovf == 0)
+        // A level wider than the skip-mask scratch only loses view skipping
+        // for its excess parents (results are unchanged): keep the result and
+        // grow the scratch for the next request.
+        if (ovf & kOverflowParents)
+            s.parent_cap *= 4;
+        if ((ovf & ~int64_t{ kOverflowParents }) == 0)
             break;
         launch_cleanup(p, st);
         s.dirty = false;

@@ -25,12 +25,16 @@ namespace
 
 constexpr int kColUnroll = 16;
 
+// Column pass.  Also flags (nonbinary != nullptr) whether any mask value,
+// as float, is neither 0 nor 1: binary masks make every SAT value an exact
+// integer, which the carve's view skipping relies on.
 template <int DT>
 __global__ void __launch_bounds__(256) sat_columns_kernel(const void* __restrict__ masks,
                                                           float* __restrict__ out,
                                                           int64_t B,
                                                           int64_t H,
-                                                          int64_t W)
+                                                          int64_t W,
+                                                          unsigned int* __restrict__ nonbinary)
 {
     const int64_t col = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (col >= B * W)
@@ -38,6 +42,7 @@ __global__ void __launch_bounds__(256) sat_columns_kernel(const void* __restrict
     const int64_t b = col / W, x = col - b * W;
     const int64_t base = b * H * W + x;
     float acc = 0.f;
+    bool nb = false;
     int64_t y = 0;
     for (; y + kColUnroll <= H; y += kColUnroll)
     {
@@ -48,15 +53,20 @@ __global__ void __launch_bounds__(256) sat_columns_kernel(const void* __restrict
 #pragma unroll
         for (int k = 0; k < kColUnroll; ++k)
         {
+            nb |= (v[k] != 0.f) & (v[k] != 1.f);
             acc = __fadd_rn(acc, v[k]);
             out[base + (y + k) * W] = acc;
         }
     }
     for (; y < H; ++y)
     {
-        acc = __fadd_rn(acc, load_f32<DT>(masks, base + y * W));
+        const float v = load_f32<DT>(masks, base + y * W);
+        nb |= (v != 0.f) & (v != 1.f);
+        acc = __fadd_rn(acc, v);
         out[base + y * W] = acc;
     }
+    if (nb && nonbinary)
+        atomicOr(nonbinary, 1u);
 }
 
 __global__ void __launch_bounds__(256) sat_rows_kernel(float* __restrict__ data, int64_t rows, int64_t W)
@@ -103,14 +113,21 @@ __global__ void convert_transforms_kernel(const void* __restrict__ tf, int64_t n
 
 } // namespace
 
-void launch_integral_image(const void* masks, int dtype, int64_t B, int64_t H, int64_t W, float* out, cudaStream_t s)
+void launch_integral_image(const void* masks,
+                           int dtype,
+                           int64_t B,
+                           int64_t H,
+                           int64_t W,
+                           float* out,
+                           cudaStream_t s,
+                           unsigned int* nonbinary)
 {
     if (B * H * W == 0)
         return;
     const int64_t cols = B * W;
     const unsigned grid = static_cast<unsigned>((cols + 255) / 256);
     bool ok = dispatch_image_dtype(dtype, [&]<int DT>() {
-        sat_columns_kernel<DT><<<grid, 256, 0, s>>>(masks, out, B, H, W);
+        sat_columns_kernel<DT><<<grid, 256, 0, s>>>(masks, out, B, H, W, nonbinary);
     });
     if (!ok)
         throw CudaError{ cudaErrorInvalidValue, "integral image: unsupported mask dtype" };

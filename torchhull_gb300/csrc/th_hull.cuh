@@ -16,6 +16,7 @@ enum OverflowBits : int64_t
     kOverflowNodes = 1,
     kOverflowCorners = 2,
     kOverflowSoup = 4,
+    kOverflowParents = 8,
 };
 
 struct DevCounters
@@ -49,6 +50,18 @@ struct HullPlan
     int64_t node_cap;
     uint8_t* child_masks; // one byte per parent of the current level
     unsigned long long* tile_sums;
+    // View skipping (binary masks only).  node_skip[k] has bit b (b < 32) set
+    // when view b need not be evaluated for the children of node k: the
+    // node's pixel box grown by one pixel lies inside the image and holds only
+    // ones, so every child is "object" there (and, for a parent of the last
+    // level in partial mode, also fully inside the frame).  child_skip holds
+    // the same masks for the 8 children of each parent of the current level.
+    uint32_t* node_skip;   // [node_cap]
+    uint32_t* child_skip;  // [parent_cap * 8]
+    uint32_t* corner_skip; // [corner_cap]: views whose bilinear factor is exactly 1
+    int64_t parent_cap;
+    const unsigned int* nonbinary; // set by the SAT pass when a mask value is not 0/1
+    bool skip_ok;                  // exact integer SAT sums (H * W < 2^24)
     // corner grid: R^3 points, one bit each, rows of WR 64-bit words (x fastest)
     int64_t R, WR;
     uint64_t* bitmap;     // [R*R*WR]

@@ -47,7 +47,15 @@ int sm_count();
 int grid_for(int64_t work_items, int threads);
 
 // Integral image (sat.cu).  masks [B,H,W] of dtype, out [B,H,W] float32.
-void launch_integral_image(const void* masks, int dtype, int64_t B, int64_t H, int64_t W, float* out, cudaStream_t s);
+// nonbinary (optional, zeroed by the caller) is set to 1 if any mask value is neither 0 nor 1.
+void launch_integral_image(const void* masks,
+                           int dtype,
+                           int64_t B,
+                           int64_t H,
+                           int64_t W,
+                           float* out,
+                           cudaStream_t s,
+                           unsigned int* nonbinary = nullptr);
 
 // Transform conversion to float32 row-major [B,16] (sat.cu).
 void launch_convert_transforms(const void* tf, int dtype, int64_t B, float* out, cudaStream_t s);
