@@ -202,6 +202,17 @@ typedef struct th_stage_times
 } th_stage_times;
 
 th_status th_context_set_profiling(th_context* ctx, int32_t enable);
+
+/* Tuning options (no reference counterpart). */
+typedef enum th_option
+{
+    /* Carve kernel per octree level: 0 = autotune (default: the first request of
+     * each size/level/mode signature is run with both kernels and the faster
+     * choice is kept), 1 = views over lanes everywhere, 2 = (parent, view) work
+     * items from level 4 on. */
+    TH_OPTION_CARVE_KERNEL = 1
+} th_option;
+th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value);
 th_status th_context_stage_times(const th_context* ctx, th_stage_times* out);
 
 /* Number of kernels this library has launched in this process (all contexts). */

@@ -9,8 +9,10 @@
 // and the request runs again, so repeated requests of similar size never allocate.
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -111,7 +113,7 @@ bool is_image_dtype(int d)
 struct HullSlot
 {
     DevBuf tf, sat, nodes, node_skip, child_masks, child_skip, tile_sums, bitmap, word_rank, rowbits, rows, corners,
-            corner_skip, values, codes, emask, soup_off, vbase, counters, flags;
+            values, codes, emask, soup_off, vbase, counters, flags;
     int64_t node_cap = 0, corner_cap = 0, parent_cap = 0;
     HullPlan plan{};
     DevCounters* host = nullptr; // pinned copy of the counters
@@ -122,9 +124,9 @@ struct HullSlot
 
     std::vector<const DevBuf*> buffers() const
     {
-        return { &tf,      &sat,  &nodes,     &node_skip,   &child_masks, &child_skip, &tile_sums,
-                 &bitmap,  &word_rank, &rowbits, &rows,   &corners,     &corner_skip, &values,
-                 &codes,   &emask, &soup_off,  &vbase,       &counters,    &flags };
+        return { &tf,     &sat,  &nodes,    &node_skip, &child_masks, &child_skip, &tile_sums,
+                 &bitmap, &word_rank, &rowbits, &rows, &corners,    &values,     &codes,
+                 &emask,  &soup_off, &vbase,   &counters, &flags };
     }
 
     void release()
@@ -186,6 +188,38 @@ struct StageEvents
 } // namespace
 } // namespace th
 
+namespace th
+{
+namespace
+{
+
+// Request signature for the carve-kernel autotuner.
+using TuneKey = std::array<int64_t, 8>;
+using CarveVariants = std::array<uint8_t, kMaxLevel>;
+
+TuneKey tune_key(const th_hull_args* a)
+{
+    return { a->batch, a->height, a->width, a->level, a->masks_partial, a->transforms_opengl, a->masks_dtype, 0 };
+}
+
+CarveVariants views_everywhere()
+{
+    CarveVariants v{};
+    return v;
+}
+
+// Work items from level 4 on (levels below have at most 8^3 parents).
+CarveVariants items_from_level4()
+{
+    CarveVariants v{};
+    for (int i = 4; i < kMaxLevel; ++i)
+        v[i] = 1;
+    return v;
+}
+
+} // namespace
+} // namespace th
+
 struct th_context
 {
     int device = 0;
@@ -196,6 +230,9 @@ struct th_context
     bool profiling = false;
     th::StageEvents events;
     th_stage_times times{};
+    int carve_mode = 0; // TH_OPTION_CARVE_KERNEL
+    std::map<th::TuneKey, th::CarveVariants> carve_tuned;
+    cudaEvent_t tune_ev[2] = { nullptr, nullptr };
 };
 
 namespace th
@@ -288,7 +325,6 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st)
     s.node_skip.ensure(sizeof(uint32_t) * node_cap);
     s.child_masks.ensure(node_cap);
     s.child_skip.ensure(sizeof(uint32_t) * 8 * parent_cap);
-    s.corner_skip.ensure(sizeof(uint32_t) * corner_cap);
     s.flags.ensure(sizeof(unsigned int) * 4);
     const int64_t scan_items = std::max({ node_cap, corner_cap, R * R });
     s.tile_sums.ensure(sizeof(unsigned long long) * ((scan_items + kScanTile - 1) / kScanTile + 1));
@@ -336,7 +372,6 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st)
     p.tile_sums = s.tile_sums.as<unsigned long long>();
     p.node_skip = s.node_skip.as<uint32_t>();
     p.child_skip = s.child_skip.as<uint32_t>();
-    p.corner_skip = s.corner_skip.as<uint32_t>();
     p.parent_cap = parent_cap;
     p.nonbinary = s.flags.as<unsigned int>();
     // exact integer box sums need every SAT sum of two entries below 2^24
@@ -388,9 +423,16 @@ void fill_info(const HullSlot& s, th_hull_info* info)
     *info = out;
 }
 
-void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t st, StageEvents* ev)
+// One complete run of a request with the given carve kernels.  carve_ms
+// (optional) receives the time of the carve stage, for the autotuner.
+void run_hull_once(th_context* ctx,
+                   HullSlot& s,
+                   const th_hull_args* a,
+                   cudaStream_t st,
+                   StageEvents* ev,
+                   const CarveVariants& variants,
+                   float* carve_ms)
 {
-    validate(a);
     if (s.dirty)
     {
         TH_CUDA(cudaStreamWaitEvent(st, s.done, 0));
@@ -402,6 +444,8 @@ void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t 
     for (int attempt = 0; attempt < 8; ++attempt)
     {
         prepare(s, a, st);
+        for (int i = 0; i < kMaxLevel; ++i)
+            s.plan.carve_variant[i] = variants[i];
         const HullPlan& p = s.plan;
         if (attempt == 0)
         {
@@ -419,6 +463,8 @@ void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t 
         // reference samples zeros everywhere), so the octree stops at the root;
         // without views nothing is refined either.  Skip the carve in both cases.
         const bool carve = p.B > 0 && p.H > 0 && p.W > 0;
+        if (carve_ms)
+            TH_CUDA(cudaEventRecord(ctx->tune_ev[0], st));
         for (int li = 0; li < p.level; ++li)
         {
             if (carve)
@@ -426,6 +472,8 @@ void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t 
             if (ev)
                 ev->record(2 + li, st);
         }
+        if (carve_ms)
+            TH_CUDA(cudaEventRecord(ctx->tune_ev[1], st));
         if (ev)
             ev->record(L + 2, st);
         launch_corners(p, st);
@@ -472,6 +520,36 @@ void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t 
         t.total_ms = ev->between(0, L + 5);
         ctx->times = t;
     }
+    if (carve_ms)
+        TH_CUDA(cudaEventElapsedTime(carve_ms, ctx->tune_ev[0], ctx->tune_ev[1]));
+}
+
+// Runs request a on slot s.  With the autotuner on, the first request of a
+// signature runs with both carve kernels (the results are identical) and the
+// faster choice is kept for later requests of that signature.
+void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t st, StageEvents* ev)
+{
+    validate(a);
+    if (ctx->carve_mode == 1)
+        return run_hull_once(ctx, s, a, st, ev, views_everywhere(), nullptr);
+    if (ctx->carve_mode == 2)
+        return run_hull_once(ctx, s, a, st, ev, items_from_level4(), nullptr);
+    const TuneKey key = tune_key(a);
+    auto it = ctx->carve_tuned.find(key);
+    if (it != ctx->carve_tuned.end())
+        return run_hull_once(ctx, s, a, st, ev, it->second, nullptr);
+    if (a->level <= 4)
+    {
+        ctx->carve_tuned[key] = views_everywhere(); // both choices coincide
+        return run_hull_once(ctx, s, a, st, ev, views_everywhere(), nullptr);
+    }
+    for (auto& e : ctx->tune_ev)
+        if (!e)
+            TH_CUDA(cudaEventCreate(&e));
+    float t_views = 0.f, t_items = 0.f;
+    run_hull_once(ctx, s, a, st, nullptr, views_everywhere(), &t_views);
+    run_hull_once(ctx, s, a, st, ev, items_from_level4(), &t_items);
+    ctx->carve_tuned[key] = (t_items < t_views) ? items_from_level4() : views_everywhere();
 }
 
 th_status fail(th_context* ctx, th_status st, const std::string& msg)
@@ -544,6 +622,9 @@ void th_context_destroy(th_context* ctx)
         s.release();
     ctx->blur_scratch.release();
     ctx->events.destroy();
+    for (auto& e : ctx->tune_ev)
+        if (e)
+            cudaEventDestroy(e);
     cudaSetDevice(prev);
     delete ctx;
 }
@@ -578,6 +659,15 @@ const char* th_status_string(th_status status)
 int64_t th_context_device_bytes(const th_context* ctx)
 {
     return ctx ? pool_bytes(ctx) : 0;
+}
+
+th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value)
+{
+    return guarded(ctx, [&] {
+        if (option != TH_OPTION_CARVE_KERNEL || value < 0 || value > 2)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "unknown option or value" };
+        ctx->carve_mode = static_cast<int>(value);
+    });
 }
 
 th_status th_context_set_profiling(th_context* ctx, int32_t enable)

@@ -5,36 +5,40 @@
 // every view; the level loop (:633-751) compacts the flags with cub and reads
 // the count back to the host.
 //
-// Work items.  A warp takes 32 parents and turns them into (parent, view)
-// items: every view of every parent except the views the parent's skip mask
-// marks (below).  Its lanes walk the item list, so skipped views cost nothing
-// and the kernel does not depend on the number of views.  A lane evaluates
-// one item: it walks the parent's 3x3x3 lattice of child corners plane by
-// plane (z), evaluating the nested fmas of the projection
-// fma(a0,x,fma(a1,y,fma(a2,z,a3))) innermost-first so the z and (y,z) partial
-// sums are shared between lattice points without changing a single rounding;
-// each plane is reduced to the pixel boxes of its four 2x2 point cells, and
-// the four children between two consecutive planes take the union of their
-// two cells (27 projections per item where the reference makes 64).  Per child
-// the per-view outcomes combine by OR (empty in any view, partial in any view,
-// fully inside some frame), so items OR their 8-bit results into the parent's
-// shared-memory slot and the result equals the reference's decision exactly.
+// Lattice.  For one parent and one view, a lane walks the parent's 3x3x3
+// lattice of child corners plane by plane (z).  The nested fmas of the
+// projection fma(a0,x,fma(a1,y,fma(a2,z,a3))) are evaluated innermost-first,
+// so the z and (y,z) partial sums are shared between lattice points without
+// changing a single rounding; each plane is reduced to the pixel boxes of its
+// four 2x2 point cells, and the four children between two consecutive planes
+// take the union of their two cells: 27 projections where the reference makes
+// 64.  Per child the per-view outcomes combine by OR (empty in any view,
+// partial in any view, fully inside some frame), so any split of the views
+// across lanes, OR-reduced, gives the reference's decision exactly.
+//
+// Two kernels share that per-(parent, view) routine:
+//  * views over lanes: a group of LANES lanes owns one parent, lane = view;
+//    coherent and best while every view must be evaluated;
+//  * (parent, view) items: a warp takes a chunk of parents, lists the views
+//    each parent still needs (below) and deals the items out to its lanes;
+//    results are OR-reduced over runs of lanes of the same parent, then
+//    merged in shared memory.  Best when many views are skipped.
+// The host picks one per level (autotuned by measuring both).
 //
 // View skipping (binary masks).  When a child's pixel box grown by one pixel
 // lies inside the image and holds only ones, the child's own children are
 // "object" in that view too: their corners project into the child's box up to
 // rounding errors far below a pixel, so their rounded boxes stay inside the
 // grown box, every pixel there is 1, and "object" contributes nothing to the
-// decision.  The child records that view in its skip mask and its children
-// never evaluate it.  Before the last level in partial mode a skipped view
-// must also report "fully inside", so there the rule additionally requires
-// every corner of the child to round at least two pixels inside the frame.
-// For leaves the mask tells the hull field that the view's bilinear factor is
-// exactly 1.  All corners must be in front of the camera for any of this.
+// decision.  The child records the view in its skip mask and the item kernel
+// never evaluates it for its children.  Before the last level in partial mode
+// a skipped view must also report "fully inside", so there the rule also
+// requires every corner of the child to round at least two pixels inside the
+// frame.  All corners must be in front of the camera for any of this.
 //
 // Conversions: the reference converts the rounded pixel coordinates to int64
 // (glm::i64vec2).  On GB300 64-bit float<->int conversions run on the FP64
-// pipe, which made them the bottleneck, so the kernel converts to int32 with
+// pipe, which made them the bottleneck, so the kernels convert to int32 with
 // saturation instead.  Every use of those values is a clamp to [0, size-1] or
 // an in-image test, whose outcome is the same for the int64 and the saturated
 // int32 value (including +-inf and NaN).  The one exception is partial mode's
@@ -57,7 +61,7 @@ namespace th
 namespace
 {
 
-constexpr int kWarps = 8; // warps per block of the classify kernel
+constexpr int kWarps = 8; // warps per block of the classify kernels
 
 __global__ void hull_init_kernel(HullPlan p)
 {
@@ -122,8 +126,8 @@ struct ViewResult
 
 // One child in one view from its pixel box (visual_hull_cuda.cu:236-285 and
 // :365-410).  The box starts the reference's min/max from +-FLT_MAX.
-// want_skip: evaluate the skip rule (binary masks, corners in front, inside
-// rule already checked by the caller).  H, W >= 1.
+// want_skip: evaluate the skip rule (the caller checked corners in front and,
+// if needed, two pixels inside).  H, W >= 1.
 template <bool PARTIAL>
 __device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sat_b, int32_t H, int32_t W, Box bb, bool want_skip)
 {
@@ -192,8 +196,24 @@ struct ItemResult
     uint32_t empty, refine, inside, skip; // 8-bit child masks
 };
 
+// World coordinates of the parent's lattice: c + v/r * L with the product
+// fused (visual_hull_cuda.cu:206-213); v/r == v * (1/r) exactly (r = 2^k).
+__device__ __forceinline__ void lattice_world(const HullPlan& p, int64_t idx, int li, float inv_rc, float wx[3], float wy[3], float wz[3])
+{
+    const int64_t mask = (int64_t{ 1 } << li) - 1;
+    const int64_t gx = idx & mask, gy = (idx >> li) & mask, gz = idx >> (2 * li);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+        wx[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gx + d), inv_rc), p.length, p.corner[0]);
+        wy[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gy + d), inv_rc), p.length, p.corner[1]);
+        wz[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gz + d), inv_rc), p.length, p.corner[2]);
+    }
+}
+
 // One (parent, view) item: the parent's lattice projected into view b.
-// skip_inside: the skip rule also needs the child's corners two pixels inside.
+// want_skip: compute the children's skip bits; skip_inside: the skip rule also
+// needs the child's corners two pixels inside the frame.
 template <bool PARTIAL, bool OPENGL>
 __device__ __forceinline__ ItemResult classify_item(const HullPlan& p,
                                                     int64_t b,
@@ -311,6 +331,101 @@ __device__ __forceinline__ ItemResult classify_item(const HullPlan& p,
     return out;
 }
 
+// Per-level constants shared by both kernels.
+struct LevelInfo
+{
+    int64_t n;
+    const int64_t* parents;
+    const uint32_t* parent_skip;
+    float inv_rc;
+    bool last;
+    bool skips;       // binary masks: skip masks are valid and may be produced
+    bool produce;     // compute the children's skip masks (the next level consumes them)
+    bool skip_inside; // the children's skip masks are for the last level (partial)
+};
+
+__device__ __forceinline__ LevelInfo level_info(const HullPlan& p, int li, bool partial)
+{
+    LevelInfo L;
+    const DevCounters* ctr = p.ctr;
+    L.n = ctr->level_count[li];
+    const int64_t off = ctr->level_off[li];
+    L.parents = p.nodes + off;
+    L.parent_skip = p.node_skip + off;
+    L.inv_rc = __fdiv_rn(1.f, static_cast<float>(int64_t{ 2 } << li)); // exact: a power of two
+    L.last = (li == p.level - 1);
+    L.skips = p.skip_ok && (*p.nonbinary == 0);
+    // the children are parents of the next level, which uses the item kernel
+    L.produce = L.skips && (li + 1 < p.level) && p.carve_variant[li + 1] == 1;
+    L.skip_inside = partial && (li + 1 == p.level - 1);
+    return L;
+}
+
+__device__ __forceinline__ void store_parent(const HullPlan& p, const LevelInfo& L, int64_t pi, uint32_t empty, uint32_t refine, uint32_t inside, bool partial)
+{
+    uint32_t mask = refine & ~empty;
+    if (partial && L.last)
+        mask &= inside;
+    p.child_masks[pi] = static_cast<uint8_t>(mask);
+}
+
+// Views over lanes: a group of LANES lanes owns one parent.
+template <int LANES, bool PARTIAL, bool OPENGL>
+__global__ void __launch_bounds__(32 * kWarps) classify_views_kernel(HullPlan p, int li)
+{
+    constexpr int G = 32 / LANES;
+    const LevelInfo L = level_info(p, li, PARTIAL);
+    const int lane = threadIdx.x & 31;
+    const int sub = lane % LANES, grp = lane / LANES;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    // skip masks can come out of a ballot only when lane == view (<= 32 views)
+    const bool produce = L.produce && LANES == 32 && p.B <= 32;
+    for (int64_t base = warp * G; base < L.n; base += nwarps * G)
+    {
+        const int64_t pi = base + grp;
+        const bool valid = pi < L.n;
+        uint32_t empty = 0, refine = 0, inside = 0, skip = 0;
+        if (valid)
+        {
+            float wx[3], wy[3], wz[3];
+            lattice_world(p, L.parents[pi], li, L.inv_rc, wx, wy, wz);
+            for (int64_t b = sub; b < p.B; b += LANES)
+            {
+                const ItemResult r = classify_item<PARTIAL, OPENGL>(p, b, wx, wy, wz, produce, L.skip_inside);
+                empty |= r.empty;
+                refine |= r.refine;
+                inside |= r.inside;
+                skip |= r.skip;
+            }
+        }
+        uint32_t cskip[8];
+        if (produce)
+        {
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                cskip[c] = __ballot_sync(0xffffffffu, (skip >> c) & 1u);
+        }
+#pragma unroll
+        for (int off = LANES / 2; off > 0; off >>= 1)
+        {
+            empty |= __shfl_xor_sync(0xffffffffu, empty, off);
+            refine |= __shfl_xor_sync(0xffffffffu, refine, off);
+            inside |= __shfl_xor_sync(0xffffffffu, inside, off);
+        }
+        if (valid && sub == 0)
+        {
+            store_parent(p, L, pi, empty, refine, inside, PARTIAL);
+            if (pi < p.parent_cap)
+            {
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    p.child_skip[pi * 8 + c] = produce ? cskip[c] : 0u;
+            }
+        }
+    }
+}
+
 struct WarpSlots
 {
     uint32_t empty[32], refine[32], inside[32];
@@ -325,41 +440,50 @@ __device__ __forceinline__ int select_bit(uint32_t m, int j)
     return __ffs(m) - 1;
 }
 
+// OR of v over the run of lanes with the same slot s (slots ascend over the
+// lanes); the run's first lane returns the full OR.
+__device__ __forceinline__ uint32_t run_or(uint32_t v, int s, int lane)
+{
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1)
+    {
+        const uint32_t vo = __shfl_down_sync(0xffffffffu, v, d);
+        const int so = __shfl_down_sync(0xffffffffu, s, d);
+        if (lane + d < 32 && so == s)
+            v |= vo;
+    }
+    return v;
+}
+
+// (parent, view) items: a warp deals the unskipped views of a chunk of parents
+// out to its lanes.
 template <bool PARTIAL, bool OPENGL>
-__global__ void __launch_bounds__(32 * kWarps) classify_kernel(HullPlan p, int li)
+__global__ void __launch_bounds__(32 * kWarps) classify_items_kernel(HullPlan p, int li)
 {
     __shared__ WarpSlots slots_all[kWarps];
     WarpSlots& ws = slots_all[threadIdx.x >> 5];
-    const DevCounters* ctr = p.ctr;
-    const int64_t n = ctr->level_count[li];
-    const int64_t lvl_off = ctr->level_off[li];
-    const int64_t* parents = p.nodes + lvl_off;
-    const uint32_t* parent_skip = p.node_skip + lvl_off;
+    const LevelInfo L = level_info(p, li, PARTIAL);
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-    const int64_t r = int64_t{ 1 } << li;
-    const float inv_rc = __fdiv_rn(1.f, static_cast<float>(2 * r)); // exact: a power of two
-    const bool last = (li == p.level - 1);
     const int B = static_cast<int>(p.B);
     const uint32_t view_bits = B >= 32 ? 0xffffffffu : ((1u << B) - 1u);
-    // view skipping needs exact integer SAT sums (binary masks, H*W < 2^24)
-    const bool skips = p.skip_ok && (*p.nonbinary == 0);
-    // what the children's skip masks will be used for
-    const bool skip_inside = PARTIAL && (li + 1 == p.level - 1);
+    // parents per chunk: enough chunks for every warp, at most one per lane
+    const int64_t per = (L.n + nwarps - 1) / nwarps;
+    const int ppw = static_cast<int>(per < 1 ? 1 : (per > 32 ? 32 : per));
 
-    for (int64_t base = warp * 32; base < n; base += nwarps * 32)
+    for (int64_t base = warp * ppw; base < L.n; base += nwarps * ppw)
     {
         const int64_t pi = base + lane;
-        const bool valid = pi < n;
-        const int64_t idx = valid ? parents[pi] : 0;
-        const uint32_t skipm = (valid && skips) ? (parent_skip[pi] & view_bits) : 0u;
+        const bool valid = lane < ppw && pi < L.n;
+        const int64_t idx = valid ? L.parents[pi] : 0;
+        const uint32_t skipm = (valid && L.skips) ? (L.parent_skip[pi] & view_bits) : 0u;
         const int count = valid ? (B - __popc(skipm)) : 0;
         ws.empty[lane] = 0;
         ws.refine[lane] = 0;
-        // before the last level a skipped view (partial mode) is one where
+        // a skipped view before the last level (partial mode) is one where
         // every child is fully inside the frame
-        ws.inside[lane] = (PARTIAL && last && skipm) ? 0xffu : 0u;
+        ws.inside[lane] = (PARTIAL && L.last && skipm) ? 0xffu : 0u;
 #pragma unroll
         for (int c = 0; c < 8; ++c)
             ws.cskip[lane][c] = 0;
@@ -382,50 +506,54 @@ __global__ void __launch_bounds__(32 * kWarps) classify_kernel(HullPlan p, int l
             const int es = __shfl_sync(0xffffffffu, excl, s);
             const uint32_t ms = __shfl_sync(0xffffffffu, skipm, s);
             const int64_t is = __shfl_sync(0xffffffffu, idx, s);
-            if (k >= total)
-                continue;
-            const int j = k - es;
-            const uint32_t active = view_bits & ~ms;
-            const int na = __popc(active);
-            const int b = j < na ? select_bit(active, j) : 32 + (j - na);
-            const int64_t gx = is % r, gy = is / r % r, gz = is / (r * r);
-            float wx[3], wy[3], wz[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d)
+            ItemResult res{ 0, 0, 0, 0 };
+            int b = 0;
+            const bool act = k < total;
+            if (act)
             {
-                // c + v/r * L fused (visual_hull_cuda.cu:206-213); v/r == v * (1/r) exactly
-                wx[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gx + d), inv_rc), p.length, p.corner[0]);
-                wy[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gy + d), inv_rc), p.length, p.corner[1]);
-                wz[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gz + d), inv_rc), p.length, p.corner[2]);
+                const int j = k - es;
+                const uint32_t active = view_bits & ~ms;
+                const int na = __popc(active);
+                b = j < na ? select_bit(active, j) : 32 + (j - na);
+                float wx[3], wy[3], wz[3];
+                lattice_world(p, is, li, L.inv_rc, wx, wy, wz);
+                res = classify_item<PARTIAL, OPENGL>(p, b, wx, wy, wz, L.produce && b < 32, L.skip_inside);
             }
-            const ItemResult res =
-                    classify_item<PARTIAL, OPENGL>(p, b, wx, wy, wz, skips && b < 32, skip_inside);
-            if (res.empty)
-                atomicOr(&ws.empty[s], res.empty);
-            if (res.refine)
-                atomicOr(&ws.refine[s], res.refine);
-            if (res.inside)
-                atomicOr(&ws.inside[s], res.inside);
-            if (res.skip)
+            const int seg = act ? s : -1 - lane;
+            const int prev_seg = __shfl_up_sync(0xffffffffu, seg, 1);
+            const bool head = act && (lane == 0 || prev_seg != seg);
+            const uint32_t e_or = run_or(res.empty, seg, lane);
+            const uint32_t r_or = run_or(res.refine, seg, lane);
+            const uint32_t i_or = run_or(res.inside, seg, lane);
+            if (head)
+            {
+                if (e_or)
+                    atomicOr(&ws.empty[s], e_or);
+                if (r_or)
+                    atomicOr(&ws.refine[s], r_or);
+                if (i_or)
+                    atomicOr(&ws.inside[s], i_or);
+            }
+            if (L.produce)
             {
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
-                    if (res.skip >> c & 1u)
-                        atomicOr(&ws.cskip[s][c], 1u << b);
+                {
+                    const uint32_t v = run_or(((res.skip >> c) & 1u) << (b & 31), seg, lane);
+                    if (head && v)
+                        atomicOr(&ws.cskip[s][c], v);
+                }
             }
         }
         __syncwarp();
         if (valid)
         {
-            uint32_t mask = ws.refine[lane] & ~ws.empty[lane];
-            if (PARTIAL && last)
-                mask &= ws.inside[lane];
-            p.child_masks[pi] = static_cast<uint8_t>(mask);
+            store_parent(p, L, pi, ws.empty[lane], ws.refine[lane], ws.inside[lane], PARTIAL);
             if (pi < p.parent_cap)
             {
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
-                    p.child_skip[pi * 8 + c] = skips ? ws.cskip[lane][c] : 0u;
+                    p.child_skip[pi * 8 + c] = L.produce ? ws.cskip[lane][c] : 0u;
             }
         }
         __syncwarp();
@@ -450,9 +578,10 @@ struct ChildEmit
         if (cnt == 0)
             return;
         const DevCounters* c = p.ctr;
-        const int64_t r = int64_t{ 1 } << li, rc = 2 * r;
+        const int64_t mask = (int64_t{ 1 } << li) - 1;
         const int64_t idx = p.nodes[c->level_off[li] + i];
-        const int64_t gx = 2 * (idx % r), gy = 2 * (idx / r % r), gz = 2 * (idx / (r * r));
+        const int64_t gx = 2 * (idx & mask), gy = 2 * ((idx >> li) & mask), gz = 2 * (idx >> (2 * li));
+        const int sh = li + 1; // children ravel at resolution 2^(li+1)
         const uint32_t m = p.child_masks[i];
         const bool has_skip = i < p.parent_cap;
         int64_t out = c->level_off[li + 1] + static_cast<int64_t>(off);
@@ -463,7 +592,7 @@ struct ChildEmit
             {
                 if (out < p.node_cap)
                 {
-                    p.nodes[out] = (gx + (k & 1)) + (gy + (k >> 1 & 1)) * rc + (gz + (k >> 2 & 1)) * rc * rc;
+                    p.nodes[out] = (gx + (k & 1)) | ((gy + (k >> 1 & 1)) << sh) | ((gz + (k >> 2 & 1)) << (2 * sh));
                     p.node_skip[out] = has_skip ? p.child_skip[i * 8 + k] : 0u;
                 }
                 ++out;
@@ -483,7 +612,7 @@ struct ChildEpilogue
         const int64_t start = ctr->level_off[li + 1];
         int64_t n = static_cast<int64_t>(total);
         if (ctr->level_count[li] > parent_cap)
-            ctr->overflow |= kOverflowParents; // skip masks were dropped; rerun with more room
+            ctr->overflow |= kOverflowParents; // skip masks were dropped for the excess
         if (start + n > node_cap)
         {
             ctr->overflow |= kOverflowNodes;
@@ -493,6 +622,27 @@ struct ChildEpilogue
         ctr->level_off[li + 2] = start + n;
     }
 };
+
+template <bool PARTIAL, bool OPENGL>
+void launch_classify(const HullPlan& p, int li, int64_t max_parents, cudaStream_t s)
+{
+    const int threads = 32 * kWarps;
+    if (p.carve_variant[li] == 1)
+    {
+        // about one lane per (parent, view) item when the level is small
+        classify_items_kernel<PARTIAL, OPENGL><<<grid_for(max_parents * p.B, threads), threads, 0, s>>>(p, li);
+        return;
+    }
+    const int grid = grid_for(max_parents * 32, threads);
+    if (p.B <= 4)
+        classify_views_kernel<4, PARTIAL, OPENGL><<<grid, threads, 0, s>>>(p, li);
+    else if (p.B <= 8)
+        classify_views_kernel<8, PARTIAL, OPENGL><<<grid, threads, 0, s>>>(p, li);
+    else if (p.B <= 16)
+        classify_views_kernel<16, PARTIAL, OPENGL><<<grid, threads, 0, s>>>(p, li);
+    else
+        classify_views_kernel<32, PARTIAL, OPENGL><<<grid, threads, 0, s>>>(p, li);
+}
 
 } // namespace
 
@@ -515,20 +665,19 @@ void launch_carve_level(const HullPlan& p, int li, cudaStream_t s)
     // Upper bound of the parents at level li, for the grid size only.
     const int64_t bound = li < 10 ? (int64_t{ 1 } << (3 * li)) : p.node_cap;
     const int64_t max_parents = bound < p.node_cap ? bound : p.node_cap;
-    const int grid = grid_for(max_parents * 8, 32 * kWarps);
     if (p.partial)
     {
         if (p.opengl)
-            classify_kernel<true, true><<<grid, 32 * kWarps, 0, s>>>(p, li);
+            launch_classify<true, true>(p, li, max_parents, s);
         else
-            classify_kernel<true, false><<<grid, 32 * kWarps, 0, s>>>(p, li);
+            launch_classify<true, false>(p, li, max_parents, s);
     }
     else
     {
         if (p.opengl)
-            classify_kernel<false, true><<<grid, 32 * kWarps, 0, s>>>(p, li);
+            launch_classify<false, true>(p, li, max_parents, s);
         else
-            classify_kernel<false, false><<<grid, 32 * kWarps, 0, s>>>(p, li);
+            launch_classify<false, false>(p, li, max_parents, s);
     }
     TH_LAUNCH_CHECK();
     run_scan(ChildCount{ p.child_masks }, ChildEmit{ p, li }, ChildEpilogue{ p.ctr, li, p.node_cap, p.parent_cap },

@@ -172,7 +172,6 @@ struct CornerEmit
                 {
                     p.corners[out] = w * 64 + bit + row * p.R;
                     p.emask[out] = 0;
-                    p.corner_skip[out] = 0;
                 }
                 ++out;
                 word &= word - 1;
@@ -237,45 +236,9 @@ __device__ __forceinline__ float view_factor(const HullPlan& p, int64_t b, float
     return bilerp(v00, v10, v01, v11, ty, tx);
 }
 
-// Views whose bilinear factor is exactly 1 for a corner: a leaf cell holding
-// the corner recorded the view in its skip mask (its box grown by a pixel is
-// inside the image and all ones, so the corner's 2x2 footprint is all ones
-// and lerp(1, 1, t) == 1 for t in [0, 1)).  Each leaf ORs its mask into its
-// eight corners.
-__global__ void __launch_bounds__(256) leaf_skip_kernel(HullPlan p)
-{
-    const DevCounters* c = p.ctr;
-    const int L = p.level;
-    const int64_t n = c->level_count[L];
-    const int64_t ncorners = c->corners;
-    const int64_t* leaves = p.nodes + c->level_off[L];
-    const uint32_t* skips = p.node_skip + c->level_off[L];
-    const int64_t r = int64_t{ 1 } << L;
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
-    {
-        const uint32_t m = skips[t];
-        if (!m)
-            continue;
-        const int64_t idx = leaves[t];
-        const int64_t x = idx % r, y = idx / r % r, z = idx / (r * r);
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-        {
-            uint32_t rank = 0;
-            if (corner_rank(p, x + (i & 1), y + (i >> 1 & 1), z + (i >> 2 & 1), rank) && rank < ncorners)
-            {
-                if ((p.corner_skip[rank] & m) != m)
-                    atomicOr(p.corner_skip + rank, m);
-            }
-        }
-    }
-}
-
 // accumulate_hull_counts_{full,partial} (visual_hull_cuda.cu:419-520): all
 // views in one thread, multiplied in ascending view order; the factors of
-// consecutive views are independent, so their loads overlap.  Views with a
-// factor of exactly 1 (corner_skip) are left out: x * 1 == x.
+// consecutive views are independent, so their loads overlap.
 template <int DT, bool PARTIAL>
 __global__ void __launch_bounds__(256) field_kernel(HullPlan p)
 {
@@ -292,15 +255,10 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p)
         const float wx = __fmaf_rn(__fmul_rn(static_cast<float>(gx), inv_rc), p.length, p.corner[0]);
         const float wy = __fmaf_rn(__fmul_rn(static_cast<float>(gy), inv_rc), p.length, p.corner[1]);
         const float wz = __fmaf_rn(__fmul_rn(static_cast<float>(gz), inv_rc), p.length, p.corner[2]);
-        const uint32_t skip = p.corner_skip[t];
         float value = 1.f;
 #pragma unroll 4
         for (int64_t b = 0; b < p.B; ++b)
-        {
-            if (b < 32 && (skip >> b & 1u))
-                continue;
             value = __fmul_rn(value, view_factor<DT, PARTIAL>(p, b, wx, wy, wz, Hf, Wf));
-        }
         p.values[t] = value;
     }
 }
@@ -558,11 +516,6 @@ void launch_corners(const HullPlan& p, cudaStream_t s)
 
 void launch_field(const HullPlan& p, cudaStream_t s)
 {
-    if (p.skip_ok)
-    {
-        leaf_skip_kernel<<<grid_for(p.node_cap, 256), 256, 0, s>>>(p);
-        TH_LAUNCH_CHECK();
-    }
     const int grid = grid_for(p.corner_cap, 256);
     bool ok = dispatch_image_dtype(p.masks_dtype, [&]<int DT>() {
         if (p.partial)

@@ -56,10 +56,11 @@ struct HullPlan
     // ones, so every child is "object" there (and, for a parent of the last
     // level in partial mode, also fully inside the frame).  child_skip holds
     // the same masks for the 8 children of each parent of the current level.
-    uint32_t* node_skip;   // [node_cap]
-    uint32_t* child_skip;  // [parent_cap * 8]
-    uint32_t* corner_skip; // [corner_cap]: views whose bilinear factor is exactly 1
+    uint32_t* node_skip;  // [node_cap]
+    uint32_t* child_skip; // [parent_cap * 8]
     int64_t parent_cap;
+    // carve kernel per parent level: 0 = views over lanes, 1 = (parent, view) items
+    uint8_t carve_variant[kMaxLevel];
     const unsigned int* nonbinary; // set by the SAT pass when a mask value is not 0/1
     bool skip_ok;                  // exact integer SAT sums (H * W < 2^24)
     // corner grid: R^3 points, one bit each, rows of WR 64-bit words (x fastest)

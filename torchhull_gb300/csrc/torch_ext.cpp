@@ -315,6 +315,77 @@ int64_t launch_count()
     return th_launch_count();
 }
 
+// TH_OPTION_CARVE_KERNEL: 0 autotune, 1 views over lanes, 2 (parent, view) items.
+void set_carve_kernel(int device, int mode)
+{
+    DeviceContext& dc = context_for(device);
+    std::lock_guard<std::mutex> g(dc.lock);
+    check(th_context_set_option(dc.ctx, TH_OPTION_CARVE_KERNEL, mode), dc.ctx);
+}
+
+// A context of its own (own pools), for callers that run several requests at
+// once on different streams, e.g. a serving loop with one context per slot.
+// The call runs on the current stream of the masks' device, with the GIL
+// released while the device works.
+class HullContext
+{
+public:
+    explicit HullContext(int device) : device_(device)
+    {
+        const th_status st = th_context_create(device, &ctx_);
+        TORCH_CHECK(st == TH_OK, "torchhull_gb300: cannot create a context on device ", device, ": ",
+                    th_status_string(st));
+    }
+    ~HullContext()
+    {
+        th_context_destroy(ctx_);
+    }
+    HullContext(const HullContext&) = delete;
+    HullContext& operator=(const HullContext&) = delete;
+
+    std::tuple<at::Tensor, at::Tensor> visual_hull(const at::Tensor& masks_in,
+                                                   const at::Tensor& transforms_in,
+                                                   int level,
+                                                   const std::array<float, 3>& cube_corner_bfl,
+                                                   float cube_length,
+                                                   bool masks_partial,
+                                                   const std::string& transforms_convention,
+                                                   bool unique_verts)
+    {
+        require_cuda(masks_in);
+        TORCH_CHECK(masks_in.device().index() == device_, "masks are not on this context's device");
+        at::cuda::CUDAGuard guard(masks_in.device());
+        const at::Tensor masks = masks_in.contiguous();
+        const at::Tensor transforms = transforms_in.contiguous();
+        th_hull_args a = hull_args(masks, transforms, level, cube_corner_bfl, cube_length, masks_partial,
+                                   transforms_convention, unique_verts);
+        void* stream = stream_of(masks);
+        std::lock_guard<std::mutex> g(lock_);
+        th_hull_info info{};
+        th_status st;
+        {
+            pybind11::gil_scoped_release nogil;
+            st = th_visual_hull(ctx_, &a, stream, &info);
+        }
+        check(st, ctx_);
+        const auto dev = masks.device();
+        at::Tensor verts = at::empty({ info.num_verts, 3 }, at::TensorOptions().dtype(at::kFloat).device(dev));
+        at::Tensor faces = at::empty({ info.num_faces, 3 }, at::TensorOptions().dtype(at::kLong).device(dev));
+        check(th_visual_hull_export(ctx_, verts.data_ptr<float>(), faces.data_ptr<int64_t>(), stream), ctx_);
+        return { verts, faces };
+    }
+
+    int64_t device_bytes() const
+    {
+        return th_context_device_bytes(ctx_);
+    }
+
+private:
+    int device_;
+    th_context* ctx_ = nullptr;
+    std::mutex lock_;
+};
+
 } // namespace
 
 PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
@@ -336,4 +407,11 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
     m.def("set_profiling", &set_profiling, "device"_a, "enable"_a, "Record CUDA events between hull stages.");
     m.def("stage_times", &stage_times, "device"_a, "Stage times (ms) of the last profiled visual_hull call.");
     m.def("launch_count", &launch_count, "Kernels launched by the CUDA library in this process.");
+    m.def("set_carve_kernel", &set_carve_kernel, "device"_a, "mode"_a,
+          "Carve kernel choice: 0 autotune, 1 views over lanes, 2 (parent, view) items.");
+    pybind11::class_<HullContext>(m, "HullContext", "Context with its own device pools (one request at a time).")
+            .def(pybind11::init<int>(), "device"_a)
+            .def("visual_hull", &HullContext::visual_hull, "masks"_a, "transforms"_a, "level"_a, "cube_corner_bfl"_a,
+                 "cube_length"_a, "masks_partial"_a, "transforms_convention"_a, "unique_verts"_a = true)
+            .def("device_bytes", &HullContext::device_bytes);
 }

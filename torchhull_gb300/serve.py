@@ -1,0 +1,167 @@
+"""Serving form: a continuous-batching request loop for visual hulls on one GPU.
+
+Requests (masks and transforms already on the device) are submitted at any
+time and return futures.  The server runs up to ``slots`` requests at once,
+each slot with its own resident context (SAT, octree and corner pools that
+stay allocated between requests) and its own CUDA stream, so the kernels of
+concurrent requests overlap on the device.  A request is admitted when a slot
+is free and the device memory it needs fits in the admission budget together
+with the requests already running; otherwise it waits, and later requests
+that do fit may go first (no head-of-line blocking).  Every request's result
+is identical to running it alone: the kernels are deterministic and slots
+share no state.
+
+The reference has no serving layer; this sits on top of the same C ABI as the
+drop-in ``visual_hull``.
+"""
+
+from __future__ import annotations
+
+import collections
+import concurrent.futures
+import dataclasses
+import threading
+import time
+
+import torch
+
+from . import _C
+from .scenes import HullRequest
+
+
+def _max_nodes(level: int) -> int:
+    return sum(8**i for i in range(min(level, 12) + 1))
+
+
+def estimate_bytes(req: HullRequest) -> int:
+    """Device bytes a request holds while it runs: its inputs plus the pools it needs.
+
+    Mirrors the pool sizing of the C library (csrc/capi.cu: prepare): SAT,
+    node and corner pools (capped at 16 M entries, the initial capacity) and
+    the corner bitmap with its rank words.
+    """
+    B, H, W = req.masks.shape[:3]
+    inputs = req.masks.numel() * req.masks.element_size() + req.transforms.numel() * req.transforms.element_size()
+    L = req.level
+    R = (1 << L) + 1
+    WR = (R + 63) // 64
+    nodes = min(_max_nodes(L), 1 << 24)
+    corners = min(R**3, 1 << 24)
+    parents = min(_max_nodes(L), 1 << 22)
+    sat = 4 * B * H * W
+    node_pool = nodes * (8 + 4 + 1) + parents * 32
+    corner_pool = corners * (8 + 4 + 1 + 1 + 4 + 4)
+    bitmap = R * R * WR * (8 + 4) + R * R * 4 + (R * R + 31) // 32 * 4
+    return int(inputs + sat + node_pool + corner_pool + bitmap)
+
+
+@dataclasses.dataclass
+class _Job:
+    req: HullRequest
+    future: concurrent.futures.Future
+    arrival: float
+    bytes: int
+    started: float = 0.0
+
+
+class HullServer:
+    """Continuous-batching visual-hull server on one device."""
+
+    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: float = 60e9):
+        self.device = torch.device("cuda", device)
+        self.budget = int(budget_bytes)
+        self._cv = threading.Condition()
+        self._pending: collections.deque[_Job] = collections.deque()
+        self._in_flight = 0
+        self._running_bytes = 0
+        self._closed = False
+        self.latencies_ms: list[float] = []
+        self.queue_ms: list[float] = []
+        self.completed = 0
+        self._contexts = [_C.HullContext(device) for _ in range(slots)]
+        self._streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        self._threads = [threading.Thread(target=self._worker, args=(i,), daemon=True) for i in range(slots)]
+        for t in self._threads:
+            t.start()
+
+    # -- client side ---------------------------------------------------------
+    def submit(self, req: HullRequest) -> concurrent.futures.Future:
+        """Queues a request; the future resolves to (verts, faces) on the device."""
+        need = estimate_bytes(req)
+        if need > self.budget:
+            raise ValueError(f"request needs {need} bytes, more than the admission budget {self.budget}")
+        fut: concurrent.futures.Future = concurrent.futures.Future()
+        with self._cv:
+            if self._closed:
+                raise RuntimeError("server is closed")
+            self._pending.append(_Job(req, fut, time.perf_counter(), need))
+            self._cv.notify_all()
+        return fut
+
+    def close(self) -> None:
+        with self._cv:
+            self._closed = True
+            self._cv.notify_all()
+        for t in self._threads:
+            t.join()
+
+    def __enter__(self) -> HullServer:
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
+    def stats(self) -> dict:
+        lat = sorted(self.latencies_ms)
+
+        def pct(p: float) -> float | None:
+            if not lat:
+                return None
+            return lat[min(len(lat) - 1, int(round(p / 100.0 * (len(lat) - 1))))]
+
+        return {"completed": self.completed, "p50_ms": pct(50), "p99_ms": pct(99),
+                "mean_queue_ms": (sum(self.queue_ms) / len(self.queue_ms)) if self.queue_ms else None,
+                "pool_bytes": sum(c.device_bytes() for c in self._contexts)}
+
+    # -- server side ---------------------------------------------------------
+    def _admit(self) -> _Job | None:
+        """First pending job that fits the budget (called with the lock held)."""
+        for i, job in enumerate(self._pending):
+            if self._running_bytes + job.bytes <= self.budget or self._in_flight == 0:
+                del self._pending[i]
+                return job
+        return None
+
+    def _worker(self, slot: int) -> None:
+        ctx, stream = self._contexts[slot], self._streams[slot]
+        while True:
+            with self._cv:
+                job = None
+                while job is None:
+                    job = self._admit()
+                    if job is None:
+                        if self._closed and not self._pending:
+                            return
+                        self._cv.wait()
+                self._in_flight += 1
+                self._running_bytes += job.bytes
+            job.started = time.perf_counter()
+            try:
+                r = job.req
+                with torch.cuda.stream(stream):
+                    verts, faces = ctx.visual_hull(r.masks, r.transforms, r.level, r.cube_corner_bfl, r.cube_length,
+                                                   r.masks_partial, r.transforms_convention, r.unique_verts)
+                stream.synchronize()
+                done = time.perf_counter()
+                job.future.set_result((verts, faces))
+                with self._cv:
+                    self.latencies_ms.append(1000.0 * (done - job.arrival))
+                    self.queue_ms.append(1000.0 * (job.started - job.arrival))
+                    self.completed += 1
+            except Exception as exc:  # surfaced to the caller through the future
+                job.future.set_exception(exc)
+            finally:
+                with self._cv:
+                    self._in_flight -= 1
+                    self._running_bytes -= job.bytes
+                    self._cv.notify_all()
