@@ -140,6 +140,7 @@ def run_gb300(args) -> dict | None:
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
 
+    th._C.set_carve_kernel(local, {"auto": 0, "views": 1, "items": 2}[args.carve_kernel])
     Q = args.requests
     reqs = [scenes.partial_request(device=dev, seed=3 + 1000 * rank + q) for q in range(Q)]
     torch.cuda.synchronize()
@@ -370,6 +371,8 @@ def main() -> None:
     ap.add_argument("--requests", type=int, default=4)
     ap.add_argument("--cpu-samples", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--carve-kernel", choices=["auto", "views", "items"], default="auto",
+                    help="carve kernel: autotuned (default) or forced")
     args = ap.parse_args()
     line = run_reference(args) if args.impl == "reference" else run_gb300(args)
     if line is not None:

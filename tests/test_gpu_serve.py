@@ -1,0 +1,61 @@
+"""Serving form: results in the mix equal results alone; admission by memory budget."""
+
+from __future__ import annotations
+
+import pytest
+import torch
+
+from torchhull_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def requests(cuda):
+    out = []
+    for i, (views, side, level, partial) in enumerate(
+            [(6, 128, 5, False), (12, 192, 6, True), (4, 96, 4, False), (9, 160, 6, False), (16, 256, 7, True),
+             (5, 128, 5, True), (8, 256, 6, False), (20, 128, 6, True)]):
+        out.append(scenes.make_request(300 + i, views, side, level, partial, device=cuda))
+    return out
+
+
+def alone(th, r):
+    v, f = th.visual_hull(**r.kwargs())
+    torch.cuda.synchronize()
+    return v.cpu(), f.cpu()
+
+
+def test_results_in_the_mix_equal_results_alone(th, cuda, requests):
+    from torchhull_gb300.serve import HullServer
+
+    expected = [alone(th, r) for r in requests]
+    with HullServer(device=cuda.index or 0, slots=3, budget_bytes=20e9) as server:
+        futures = [server.submit(r) for r in requests + requests]
+        got = [f.result(timeout=120) for f in futures]
+        stats = server.stats()
+    for k, (v, f) in enumerate(got):
+        ev, ef = expected[k % len(requests)]
+        assert torch.equal(v.cpu(), ev) and torch.equal(f.cpu(), ef), k
+    assert stats["completed"] == 2 * len(requests)
+    assert stats["p50_ms"] is not None and stats["p99_ms"] >= stats["p50_ms"]
+
+
+def test_tight_budget_admits_one_at_a_time(th, cuda, requests):
+    from torchhull_gb300.serve import HullServer, estimate_bytes
+
+    budget = max(estimate_bytes(r) for r in requests)  # room for one request at a time
+    with HullServer(device=cuda.index or 0, slots=3, budget_bytes=budget) as server:
+        futures = [server.submit(r) for r in requests[:4]]
+        got = [f.result(timeout=120) for f in futures]
+    for r, (v, f) in zip(requests[:4], got, strict=True):
+        ev, ef = alone(th, r)
+        assert torch.equal(v.cpu(), ev) and torch.equal(f.cpu(), ef)
+
+
+def test_request_larger_than_budget_is_refused(cuda, requests):
+    from torchhull_gb300.serve import HullServer
+
+    with HullServer(device=cuda.index or 0, slots=1, budget_bytes=1e6) as server:
+        with pytest.raises(ValueError):
+            server.submit(requests[0])

@@ -750,8 +750,7 @@ th_status th_visual_hull_export_field(th_context* ctx, int64_t* indices, float* 
         {
             if (!indices || !values)
                 throw ArgError{ TH_ERR_INVALID_ARGUMENT, "indices or values pointer is NULL" };
-            TH_CUDA(cudaMemcpyAsync(indices, s.plan.corners, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, st));
-            TH_CUDA(cudaMemcpyAsync(values, s.plan.values, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+            launch_export_field(s.plan, n, indices, values, st);
         }
         TH_CUDA(cudaEventRecord(s.done, st));
     });

@@ -160,6 +160,8 @@ struct CornerEmit
     {
         const int64_t row = p.rows[k];
         const int64_t base = row * p.WR;
+        const uint32_t ry = static_cast<uint32_t>(row) % static_cast<uint32_t>(p.R);
+        const uint32_t rz = static_cast<uint32_t>(row) / static_cast<uint32_t>(p.R);
         uint64_t out = off;
         for (int64_t w = 0; w < p.WR; ++w)
         {
@@ -170,7 +172,7 @@ struct CornerEmit
                 const int bit = __ffsll(static_cast<long long>(word)) - 1;
                 if (static_cast<int64_t>(out) < p.corner_cap)
                 {
-                    p.corners[out] = w * 64 + bit + row * p.R;
+                    p.corners[out] = pack_corner(w * 64 + bit, ry, rz);
                     p.emask[out] = 0;
                 }
                 ++out;
@@ -250,7 +252,8 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p)
     for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
     {
         const int64_t idx = p.corners[t];
-        const int64_t gx = idx % R, gy = idx / R % R, gz = idx / (R * R);
+        int64_t gx, gy, gz;
+        unpack_corner(idx, gx, gy, gz);
         // c + v/r * L fused (visual_hull_cuda.cu:444-448); v/r == v * (1/r) exactly
         const float wx = __fmaf_rn(__fmul_rn(static_cast<float>(gx), inv_rc), p.length, p.corner[0]);
         const float wy = __fmaf_rn(__fmul_rn(static_cast<float>(gy), inv_rc), p.length, p.corner[1]);
@@ -291,13 +294,13 @@ __global__ void __launch_bounds__(256) mc_cells_kernel(HullPlan p)
     __shared__ TableCache tab;
     load_tables(tab);
     const int64_t n = p.ctr->corners;
-    const int64_t R = p.R;
     const float iso = 0.5f;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
     {
         const int64_t idx = p.corners[t];
-        const int64_t gx = idx % R, gy = idx / R % R, gz = idx / (R * R);
+        int64_t gx, gy, gz;
+        unpack_corner(idx, gx, gy, gz);
         uint32_t rk[8];
         uint32_t code = 0;
         if (cell_ranks(p, t, n, gx, gy, gz, rk))
@@ -410,7 +413,6 @@ __device__ __forceinline__ void edge_vertex(const HullPlan& p,
 __global__ void __launch_bounds__(256) export_verts_kernel(HullPlan p, float* __restrict__ verts)
 {
     const int64_t n = p.ctr->corners;
-    const int64_t R = p.R;
     const float scale = __fdiv_rn(p.length, static_cast<float>(int64_t{ 1 } << p.level));
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
@@ -419,7 +421,8 @@ __global__ void __launch_bounds__(256) export_verts_kernel(HullPlan p, float* __
         if (!bits)
             continue;
         const int64_t idx = p.corners[t];
-        const int64_t gx = idx % R, gy = idx / R % R, gz = idx / (R * R);
+        int64_t gx, gy, gz;
+        unpack_corner(idx, gx, gy, gz);
         const float v1 = p.values[t];
         int64_t out = p.vbase[t];
 #pragma unroll
@@ -447,7 +450,6 @@ __global__ void __launch_bounds__(256) export_faces_kernel(HullPlan p, float* __
     __shared__ TableCache tab;
     load_tables(tab);
     const int64_t n = p.ctr->corners;
-    const int64_t R = p.R;
     const float scale = __fdiv_rn(p.length, static_cast<float>(int64_t{ 1 } << p.level));
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
@@ -457,7 +459,8 @@ __global__ void __launch_bounds__(256) export_faces_kernel(HullPlan p, float* __
         if (cnt == 0)
             continue;
         const int64_t idx = p.corners[t];
-        const int64_t gx = idx % R, gy = idx / R % R, gz = idx / (R * R);
+        int64_t gx, gy, gz;
+        unpack_corner(idx, gx, gy, gz);
         uint32_t rk[8];
         cell_ranks(p, t, n, gx, gy, gz, rk);
         const int64_t base = p.soup_off[t];
@@ -545,6 +548,32 @@ void launch_export(const HullPlan& p, float* verts, int64_t* faces, cudaStream_t
         TH_LAUNCH_CHECK();
     }
     export_faces_kernel<<<grid, 256, 0, s>>>(p, verts, faces);
+    TH_LAUNCH_CHECK();
+}
+
+namespace
+{
+
+__global__ void __launch_bounds__(256) export_field_kernel(HullPlan p, int64_t n, int64_t* __restrict__ indices, float* __restrict__ values)
+{
+    const int64_t R = p.R;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
+    {
+        int64_t x, y, z;
+        unpack_corner(p.corners[t], x, y, z);
+        indices[t] = x + y * R + z * R * R;
+        values[t] = p.values[t];
+    }
+}
+
+} // namespace
+
+void launch_export_field(const HullPlan& p, int64_t n, int64_t* indices, float* values, cudaStream_t s)
+{
+    if (n <= 0)
+        return;
+    export_field_kernel<<<grid_for(n, 256), 256, 0, s>>>(p, n, indices, values);
     TH_LAUNCH_CHECK();
 }
 

@@ -1,0 +1,285 @@
+// Per-(parent, view) carve routine shared by the plain and the batched
+// carve kernels: the 3x3x3 lattice of a parent projected into one view and
+// the classification of its eight children (see carve.cu for the design).
+#pragma once
+
+#include <cfloat>
+
+#include "th_common.cuh"
+
+namespace th
+{
+
+struct Box
+{
+    float minx, miny, maxx, maxy;
+};
+
+__device__ __forceinline__ Box merge(const Box& a, const Box& b)
+{
+    return Box{ fminf(a.minx, b.minx), fminf(a.miny, b.miny), fmaxf(a.maxx, b.maxx), fmaxf(a.maxy, b.maxy) };
+}
+
+// Saturating float -> int32 (NaN to a value outside every image).
+__device__ __forceinline__ int32_t f2i32(float f)
+{
+    return __float2int_rz(f);
+}
+
+__device__ __forceinline__ bool fits_i32(float f)
+{
+    return f > -2147483648.0f && f < 2147483648.0f;
+}
+
+__device__ __forceinline__ float box_sum(const float* __restrict__ sat_b, int32_t W, int32_t x0, int32_t y0, int32_t x1, int32_t y1)
+{
+    // sample_zeros_padding at the four corners (image_utils.h:84-97); inputs are
+    // clamped to the image, so only the -1 row/column can leave it.
+    const float* row_hi = sat_b + static_cast<int64_t>(y1) * W;
+    const float* row_lo = sat_b + static_cast<int64_t>(y0 - 1) * W;
+    const float i11 = row_hi[x1];
+    const float i10 = x0 > 0 ? row_hi[x0 - 1] : 0.f;
+    const float i01 = y0 > 0 ? row_lo[x1] : 0.f;
+    const float i00 = (x0 > 0 && y0 > 0) ? row_lo[x0 - 1] : 0.f;
+    return __fsub_rn(__fsub_rn(__fadd_rn(i11, i00), i10), i01);
+}
+
+enum ViewClass : uint32_t
+{
+    kNone = 0,
+    kEmpty = 1,
+    kRefine = 2,
+    kObject = 3,
+};
+
+struct ViewResult
+{
+    uint32_t cls;
+    bool skip; // the child's children may skip this view
+};
+
+// One child in one view from its pixel box (visual_hull_cuda.cu:236-285 and
+// :365-410).  The box starts the reference's min/max from +-FLT_MAX.
+// want_skip: evaluate the skip rule (the caller checked corners in front and,
+// if needed, two pixels inside).  H, W >= 1.
+template <bool PARTIAL>
+__device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sat_b, int32_t H, int32_t W, Box bb, bool want_skip)
+{
+    const float margin = 0.5f - 0.1f; // isolevel - epsilon (visual_hull_cuda.cu:259-267)
+    bb.minx = fminf(FLT_MAX, bb.minx);
+    bb.miny = fminf(FLT_MAX, bb.miny);
+    bb.maxx = fmaxf(-FLT_MAX, bb.maxx);
+    bb.maxy = fmaxf(-FLT_MAX, bb.maxy);
+    const float fminx = roundf(__fadd_rn(bb.minx, -0.5f));
+    const float fminy = roundf(__fadd_rn(bb.miny, -0.5f));
+    const float fmaxx = roundf(__fadd_rn(bb.maxx, 0.5f));
+    const float fmaxy = roundf(__fadd_rn(bb.maxy, 0.5f));
+    const int32_t cminx = min(max(f2i32(fminx), 0), W - 1);
+    const int32_t cminy = min(max(f2i32(fminy), 0), H - 1);
+    const int32_t cmaxx = min(max(f2i32(fmaxx), 0), W - 1);
+    const int32_t cmaxy = min(max(f2i32(fmaxy), 0), H - 1);
+    const int64_t area = static_cast<int64_t>(cmaxy - cminy + 1) * static_cast<int64_t>(cmaxx - cminx + 1);
+    const float sum = box_sum(sat_b, W, cminx, cminy, cmaxx, cmaxy);
+    bool whole = true;
+    if (PARTIAL)
+    {
+        // full_area_bb (:377) from the unclamped rounded box, int64 arithmetic
+        // wrapping like the device's; exact int64 values when int32 cannot hold them.
+        int64_t rminx, rminy, rmaxx, rmaxy;
+        if (fits_i32(fminx) && fits_i32(fminy) && fits_i32(fmaxx) && fits_i32(fmaxy))
+        {
+            rminx = f2i32(fminx);
+            rminy = f2i32(fminy);
+            rmaxx = f2i32(fmaxx);
+            rmaxy = f2i32(fmaxy);
+        }
+        else
+        {
+            rminx = f2i64(fminx);
+            rminy = f2i64(fminy);
+            rmaxx = f2i64(fmaxx);
+            rmaxy = f2i64(fmaxy);
+        }
+        const uint64_t fy = static_cast<uint64_t>(rmaxy) - static_cast<uint64_t>(rminy) + 1u;
+        const uint64_t fx = static_cast<uint64_t>(rmaxx) - static_cast<uint64_t>(rminx) + 1u;
+        whole = (static_cast<uint64_t>(area) == fy * fx);
+    }
+    const float area_f = (area >= INT32_MIN && area <= INT32_MAX) ? __int2float_rn(static_cast<int32_t>(area))
+                                                                  : __ll2float_rn(area);
+    ViewResult res{ kNone, false };
+    if (sum <= 0.f + margin && whole)
+        res.cls = kEmpty;
+    else if (sum >= __fsub_rn(area_f, margin) && whole)
+        res.cls = kObject;
+    else if (!PARTIAL || (cmaxy - cminy > 1 && cmaxx - cminx > 1))
+        res.cls = kRefine;
+    if (want_skip && res.cls == kObject && fminx >= 1.f && fminy >= 1.f && fmaxx <= static_cast<float>(W - 2) &&
+        fmaxy <= static_cast<float>(H - 2))
+    {
+        // the box grown by one pixel is inside the image: all ones there?
+        const int32_t x0 = static_cast<int32_t>(fminx) - 1, y0 = static_cast<int32_t>(fminy) - 1;
+        const int32_t x1 = static_cast<int32_t>(fmaxx) + 1, y1 = static_cast<int32_t>(fmaxy) + 1;
+        const float grown = box_sum(sat_b, W, x0, y0, x1, y1);
+        res.skip = grown == static_cast<float>((y1 - y0 + 1) * (x1 - x0 + 1));
+    }
+    return res;
+}
+
+struct ItemResult
+{
+    uint32_t empty, refine, inside, skip; // 8-bit child masks
+};
+
+// World coordinates of the lattice of the cell idx (ravelled at resolution
+// 2^li): c + v/r * L with the product fused (visual_hull_cuda.cu:206-213);
+// v/r == v * (1/r) exactly (r = 2^k).
+__device__ __forceinline__ void lattice_world(const float corner[3],
+                                              float length,
+                                              int64_t idx,
+                                              int li,
+                                              float inv_rc,
+                                              float wx[3],
+                                              float wy[3],
+                                              float wz[3])
+{
+    const int64_t mask = (int64_t{ 1 } << li) - 1;
+    const int64_t gx = idx & mask, gy = (idx >> li) & mask, gz = idx >> (2 * li);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+        wx[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gx + d), inv_rc), length, corner[0]);
+        wy[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gy + d), inv_rc), length, corner[1]);
+        wz[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gz + d), inv_rc), length, corner[2]);
+    }
+}
+
+// The per-view data an item reads.
+struct ViewSource
+{
+    const float* tf;  // [B,16] float32 transforms
+    const float* sat; // [B,H,W] integral images
+    int64_t H, W;
+};
+
+// One (parent, view) item: the parent's lattice projected into view b.
+// want_skip: compute the children's skip bits; skip_inside: the skip rule also
+// needs the child's corners two pixels inside the frame.
+template <bool PARTIAL, bool OPENGL>
+__device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
+                                                    int64_t b,
+                                                    const float wx[3],
+                                                    const float wy[3],
+                                                    const float wz[3],
+                                                    bool want_skip,
+                                                    bool skip_inside)
+{
+    const int32_t H = static_cast<int32_t>(p.H), W = static_cast<int32_t>(p.W);
+    const float Hf = static_cast<float>(p.H), Wf = static_cast<float>(p.W);
+    const float* m = p.tf + 16 * b;
+    // rows x, y and the divisor row (w for OpenGL, z for OpenCV)
+    const float4 rx = *reinterpret_cast<const float4*>(m);
+    const float4 ry = *reinterpret_cast<const float4*>(m + 4);
+    const float4 rd = *reinterpret_cast<const float4*>(m + (OPENGL ? 12 : 8));
+    const float* sat_b = p.sat + b * p.H * p.W;
+    ItemResult out{ 0, 0, 0, 0 };
+    Box prev[4];
+    uint32_t prev_in = 0, prev_in2 = 0, prev_front = 0;
+#pragma unroll
+    for (int z = 0; z < 3; ++z)
+    {
+        const float tzx = __fmaf_rn(rx.z, wz[z], rx.w);
+        const float tzy = __fmaf_rn(ry.z, wz[z], ry.w);
+        const float tzd = __fmaf_rn(rd.z, wz[z], rd.w);
+        float px[9], py[9];
+        uint32_t in9 = 0, in9b = 0, front9 = 0;
+#pragma unroll
+        for (int y = 0; y < 3; ++y)
+        {
+            const float tyx = __fmaf_rn(rx.y, wy[y], tzx);
+            const float tyy = __fmaf_rn(ry.y, wy[y], tzy);
+            const float tyd = __fmaf_rn(rd.y, wy[y], tzd);
+#pragma unroll
+            for (int x = 0; x < 3; ++x)
+            {
+                const int k = x + 3 * y;
+                const float cx = __fmaf_rn(rx.x, wx[x], tyx);
+                const float cy = __fmaf_rn(ry.x, wx[x], tyy);
+                const float cd = __fmaf_rn(rd.x, wx[x], tyd);
+                const float nx = __fdiv_rn(cx, cd);
+                const float ny = __fdiv_rn(cy, cd);
+                if (OPENGL)
+                {
+                    // (n + 1) * size / 2 - 0.5 (image_utils.h:67-71); /2 == *0.5 exactly
+                    px[k] = __fsub_rn(__fmul_rn(__fmul_rn(__fadd_rn(nx, 1.f), Wf), 0.5f), 0.5f);
+                    py[k] = __fsub_rn(__fmul_rn(__fmul_rn(__fadd_rn(ny, 1.f), Hf), 0.5f), 0.5f);
+                }
+                else
+                {
+                    px[k] = __fsub_rn(nx, 0.5f);
+                    py[k] = __fsub_rn(ny, 0.5f);
+                }
+                if (want_skip && cd > 0.f)
+                    front9 |= 1u << k;
+                if (PARTIAL)
+                {
+                    const int32_t qx = f2i32(roundf(px[k]));
+                    const int32_t qy = f2i32(roundf(py[k]));
+                    if (1 <= qy && qy < H - 1 && 1 <= qx && qx < W - 1)
+                        in9 |= 1u << k;
+                    if (skip_inside && 2 <= qy && qy < H - 2 && 2 <= qx && qx < W - 2)
+                        in9b |= 1u << k;
+                }
+            }
+        }
+        Box cur[4];
+        uint32_t cur_in = 0, cur_in2 = 0, cur_front = 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+        {
+            const int cx = c & 1, cy = c >> 1;
+            const int k0 = cx + 3 * cy, k1 = k0 + 1, k2 = k0 + 3, k3 = k0 + 4;
+            cur[c] = Box{ fminf(fminf(px[k0], px[k1]), fminf(px[k2], px[k3])),
+                          fminf(fminf(py[k0], py[k1]), fminf(py[k2], py[k3])),
+                          fmaxf(fmaxf(px[k0], px[k1]), fmaxf(px[k2], px[k3])),
+                          fmaxf(fmaxf(py[k0], py[k1]), fmaxf(py[k2], py[k3])) };
+            const uint32_t need = (1u << k0) | (1u << k1) | (1u << k2) | (1u << k3);
+            if ((in9 & need) == need)
+                cur_in |= 1u << c;
+            if ((in9b & need) == need)
+                cur_in2 |= 1u << c;
+            if ((front9 & need) == need)
+                cur_front |= 1u << c;
+        }
+        if (z > 0)
+        {
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+            {
+                const uint32_t cbit = 1u << c;
+                const uint32_t bit = 1u << (c + 4 * (z - 1));
+                const bool front = (prev_front & cur_front & cbit) != 0;
+                const bool in2 = (prev_in2 & cur_in2 & cbit) != 0;
+                const ViewResult r = classify_view<PARTIAL>(sat_b, H, W, merge(prev[c], cur[c]),
+                                                            want_skip && front && (!skip_inside || in2));
+                if (r.cls == kEmpty)
+                    out.empty |= bit;
+                else if (r.cls == kRefine)
+                    out.refine |= bit;
+                if (r.skip)
+                    out.skip |= bit;
+                if (PARTIAL && (prev_in & cur_in & cbit))
+                    out.inside |= bit;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            prev[c] = cur[c];
+        prev_in = cur_in;
+        prev_in2 = cur_in2;
+        prev_front = cur_front;
+    }
+    return out;
+}
+
+
+} // namespace th

@@ -80,7 +80,24 @@ struct HullPlan
     DevCounters* ctr;
 };
 
+// Corner ids inside the pipeline: x | y << 21 | z << 42 (grid points < 2^21
+// per axis).  Ascending packed ids are ascending ravelled ids x + y*R + z*R*R,
+// and decoding needs shifts instead of 64-bit divisions by R.
+__device__ __forceinline__ int64_t pack_corner(int64_t x, int64_t y, int64_t z)
+{
+    return x | (y << 21) | (z << 42);
+}
+
+__device__ __forceinline__ void unpack_corner(int64_t v, int64_t& x, int64_t& y, int64_t& z)
+{
+    x = v & 0x1FFFFF;
+    y = (v >> 21) & 0x1FFFFF;
+    z = v >> 42;
+}
+
 void launch_hull_init(const HullPlan& p, cudaStream_t s);
+// Sparse field export: ravelled ids (x + y*R + z*R*R) and values.
+void launch_export_field(const HullPlan& p, int64_t n, int64_t* indices, float* values, cudaStream_t s);
 void launch_carve_level(const HullPlan& p, int level_index, cudaStream_t s);
 void launch_corners(const HullPlan& p, cudaStream_t s);
 void launch_field(const HullPlan& p, cudaStream_t s);
