@@ -1,0 +1,274 @@
+// Batched form: the octrees of many requests, carved by one persistent launch.
+//
+// The plain path launches a classify kernel and a compaction per level and
+// request.  Here one cooperative kernel, resident on every SM, walks the
+// levels of all requests at once: level i is one list of request-tagged cells
+// (the device work queue).  Warps dequeue chunks of it with an atomic head,
+// deal the chunk's unskipped (cell, view) items to their lanes with the same
+// per-item routine as the plain kernels (th_classify.cuh), and append the
+// refined children, tagged, to the list of level i+1 with one atomic per warp.
+// A grid-wide barrier separates the levels.  Requests with different view
+// counts, sizes, levels and modes share warps; a cell whose request ends at
+// level i is a leaf and produces no items.  Children are appended in arrival
+// order, not the reference's order, which changes nothing downstream: the
+// corner set is built in a bitmap and comes out sorted either way, so each
+// request's mesh is bit-identical to the plain path's.
+//
+// Afterwards one launch marks the corners of every request's leaves in that
+// request's bitmap; the remaining stages (corner ranks, field, marching cubes)
+// run per request on the host's streams.
+
+#include <cooperative_groups.h>
+
+#include "th_batch.cuh"
+#include "th_classify.cuh"
+#include "th_hull.cuh"
+#include "th_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace th
+{
+
+namespace
+{
+
+constexpr int kBatchWarps = 8;
+constexpr int64_t kCellMask = (int64_t{ 1 } << kTagShift) - 1;
+
+__global__ void batch_init_kernel(BatchPlan bp)
+{
+    for (int i = threadIdx.x; i < bp.nreq; i += blockDim.x)
+    {
+        bp.nodes[i] = static_cast<int64_t>(i) << kTagShift;
+        bp.node_skip[i] = 0;
+    }
+    if (threadIdx.x == 0)
+        bp.ctr->count[0] = bp.nreq;
+}
+
+__device__ __forceinline__ ItemResult batch_item(const BatchReq& q,
+                                                 int64_t b,
+                                                 const float wx[3],
+                                                 const float wy[3],
+                                                 const float wz[3],
+                                                 bool want_skip,
+                                                 bool skip_inside)
+{
+    const ViewSource src{ q.tf, q.sat, q.H, q.W };
+    if (q.partial)
+        return q.opengl ? classify_item<true, true>(src, b, wx, wy, wz, want_skip, skip_inside)
+                        : classify_item<true, false>(src, b, wx, wy, wz, want_skip, skip_inside);
+    return q.opengl ? classify_item<false, true>(src, b, wx, wy, wz, want_skip, skip_inside)
+                    : classify_item<false, false>(src, b, wx, wy, wz, want_skip, skip_inside);
+}
+
+// Entries of level li that were written (a pool overflow drops the rest).
+__device__ __forceinline__ int64_t level_entries(const BatchPlan& bp, int li, int64_t start)
+{
+    const int64_t n = bp.ctr->count[li];
+    const int64_t room = bp.node_cap - start;
+    return n < room ? n : (room > 0 ? room : 0);
+}
+
+__global__ void __launch_bounds__(32 * kBatchWarps) batch_carve_kernel(BatchPlan bp)
+{
+    cg::grid_group grid = cg::this_grid();
+    __shared__ WarpSlots slots_all[kBatchWarps];
+    WarpSlots& ws = slots_all[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    BatchCounters* ctr = bp.ctr;
+    const int64_t nwarps = static_cast<int64_t>(gridDim.x) * kBatchWarps;
+    int64_t start = 0;
+    for (int li = 0; li < bp.max_level; ++li)
+    {
+        const int64_t n = level_entries(bp, li, start);
+        const int64_t next = start + n;
+        const float inv_rc = __fdiv_rn(1.f, static_cast<float>(int64_t{ 2 } << li)); // exact: a power of two
+        const int64_t per = (n + nwarps - 1) / nwarps;
+        const int ppw = static_cast<int>(per < 1 ? 1 : (per > 32 ? 32 : per));
+        for (;;)
+        {
+            unsigned long long got = 0;
+            if (lane == 0)
+                got = atomicAdd(&ctr->head[li], static_cast<unsigned long long>(ppw));
+            const int64_t base = static_cast<int64_t>(__shfl_sync(0xffffffffu, got, 0));
+            if (base >= n)
+                break;
+            const int64_t pi = base + lane;
+            const bool valid = lane < ppw && pi < n;
+            const int64_t node = valid ? bp.nodes[start + pi] : 0;
+            const BatchReq& q = bp.reqs[static_cast<int>(node >> kTagShift)];
+            const bool work = valid && q.level > li && !q.no_carve;
+            const bool skips = work && q.skip_ok && (*q.nonbinary == 0);
+            const uint32_t view_bits = q.B >= 32 ? 0xffffffffu : ((1u << q.B) - 1u);
+            const uint32_t skipm = skips ? (bp.node_skip[start + pi] & view_bits) : 0u;
+            const int count = work ? (q.B - __popc(skipm)) : 0;
+            const bool last = (li == q.level - 1);
+            ws.empty[lane] = 0;
+            ws.refine[lane] = 0;
+            ws.inside[lane] = (work && q.partial && last && skipm) ? 0xffu : 0u;
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                ws.cskip[lane][c] = 0;
+            const int incl = warp_inclusive_scan(count);
+            const int excl = incl - count;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            __syncwarp();
+            for (int k0 = 0; k0 < total; k0 += 32)
+            {
+                const int k = k0 + lane;
+                const int s = item_slot(excl, k);
+                const int es = __shfl_sync(0xffffffffu, excl, s);
+                const uint32_t ms = __shfl_sync(0xffffffffu, skipm, s);
+                const int64_t is = __shfl_sync(0xffffffffu, node, s);
+                const bool act = k < total;
+                ItemResult res{ 0, 0, 0, 0 };
+                int b = 0;
+                bool produce = false;
+                if (act)
+                {
+                    const BatchReq& qq = bp.reqs[static_cast<int>(is >> kTagShift)];
+                    const uint32_t vb = qq.B >= 32 ? 0xffffffffu : ((1u << qq.B) - 1u);
+                    const uint32_t active = vb & ~ms;
+                    const int na = __popc(active);
+                    const int j = k - es;
+                    b = j < na ? select_bit(active, j) : 32 + (j - na);
+                    float wx[3], wy[3], wz[3];
+                    lattice_world(qq.corner, qq.length, is & kCellMask, li, inv_rc, wx, wy, wz);
+                    produce = qq.skip_ok && (*qq.nonbinary == 0) && (li + 1 < qq.level);
+                    const bool skip_inside = qq.partial && (li + 1 == qq.level - 1);
+                    res = batch_item(qq, b, wx, wy, wz, produce && b < 32, skip_inside);
+                }
+                const int seg = act ? s : -1 - lane;
+                const int prev_seg = __shfl_up_sync(0xffffffffu, seg, 1);
+                const bool head = act && (lane == 0 || prev_seg != seg);
+                const uint32_t e_or = run_or(res.empty, seg, lane);
+                const uint32_t r_or = run_or(res.refine, seg, lane);
+                const uint32_t i_or = run_or(res.inside, seg, lane);
+                if (head)
+                {
+                    if (e_or)
+                        atomicOr(&ws.empty[s], e_or);
+                    if (r_or)
+                        atomicOr(&ws.refine[s], r_or);
+                    if (i_or)
+                        atomicOr(&ws.inside[s], i_or);
+                }
+                if (__any_sync(0xffffffffu, produce))
+                {
+#pragma unroll
+                    for (int c = 0; c < 8; ++c)
+                    {
+                        const uint32_t v = run_or(((res.skip >> c) & 1u) << (b & 31), seg, lane);
+                        if (head && v)
+                            atomicOr(&ws.cskip[s][c], v);
+                    }
+                }
+            }
+            __syncwarp();
+            // the refined children of every slot, appended to level li+1
+            uint32_t mask = 0;
+            if (work)
+            {
+                mask = ws.refine[lane] & ~ws.empty[lane];
+                if (q.partial && last)
+                    mask &= ws.inside[lane];
+            }
+            const int nch = __popc(mask);
+            const int cincl = warp_inclusive_scan(nch);
+            const int ctot = __shfl_sync(0xffffffffu, cincl, 31);
+            unsigned long long obase = 0;
+            if (lane == 0 && ctot > 0)
+                obase = atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->count[li + 1]),
+                                  static_cast<unsigned long long>(ctot));
+            obase = __shfl_sync(0xffffffffu, obase, 0);
+            if (nch)
+            {
+                const bool produce_me = skips && (li + 1 < q.level);
+                const int64_t cell = node & kCellMask;
+                const int64_t m = (int64_t{ 1 } << li) - 1;
+                const int64_t gx = 2 * (cell & m), gy = 2 * ((cell >> li) & m), gz = 2 * (cell >> (2 * li));
+                const int sh = li + 1;
+                const int64_t tag = node & ~kCellMask;
+                int64_t out = next + static_cast<int64_t>(obase) + (cincl - nch);
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                {
+                    if (!(mask >> c & 1u))
+                        continue;
+                    if (out < bp.node_cap)
+                    {
+                        bp.nodes[out] = tag | (gx + (c & 1)) | ((gy + (c >> 1 & 1)) << sh) |
+                                        ((gz + (c >> 2 & 1)) << (2 * sh));
+                        bp.node_skip[out] = produce_me ? ws.cskip[lane][c] : 0u;
+                    }
+                    else
+                        atomicOr(&ctr->overflow, 1ull);
+                    ++out;
+                }
+            }
+            __syncwarp();
+        }
+        grid.sync();
+        start = next;
+    }
+}
+
+__global__ void __launch_bounds__(256) batch_mark_kernel(BatchPlan bp)
+{
+    int64_t starts[kMaxLevel + 2];
+    int64_t s = 0;
+    for (int li = 0; li <= bp.max_level; ++li)
+    {
+        starts[li] = s;
+        s += level_entries(bp, li, s);
+    }
+    const int64_t total = s;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride)
+    {
+        int li = 0;
+        while (li < bp.max_level && starts[li + 1] <= t)
+            ++li;
+        const int64_t node = bp.nodes[t];
+        const BatchReq& q = bp.reqs[static_cast<int>(node >> kTagShift)];
+        if (q.level != li)
+            continue;
+        const int64_t cell = node & kCellMask;
+        const int64_t m = (int64_t{ 1 } << li) - 1;
+        mark_cell_corners(q.bitmap, q.rowbits, q.R, q.WR, cell & m, (cell >> li) & m, cell >> (2 * li));
+    }
+}
+
+} // namespace
+
+void launch_batch_init(const BatchPlan& bp, cudaStream_t s)
+{
+    TH_CUDA(cudaMemsetAsync(bp.ctr, 0, sizeof(BatchCounters), s));
+    batch_init_kernel<<<1, 256, 0, s>>>(bp);
+    TH_LAUNCH_CHECK();
+}
+
+void launch_batch_carve(const BatchPlan& bp, cudaStream_t s)
+{
+    if (bp.max_level <= 0)
+        return;
+    int per_sm = 0;
+    TH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_carve_kernel, 32 * kBatchWarps, 0));
+    if (per_sm < 1)
+        throw CudaError{ cudaErrorLaunchOutOfResources, "batch carve kernel does not fit on an SM" };
+    BatchPlan arg = bp;
+    void* args[] = { &arg };
+    TH_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(batch_carve_kernel), dim3(per_sm * sm_count()),
+                                        dim3(32 * kBatchWarps), args, 0, s));
+    note_launches(1);
+}
+
+void launch_batch_mark(const BatchPlan& bp, cudaStream_t s)
+{
+    batch_mark_kernel<<<grid_for(bp.node_cap, 256), 256, 0, s>>>(bp);
+    TH_LAUNCH_CHECK();
+}
+
+} // namespace th

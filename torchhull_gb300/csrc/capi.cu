@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "th_batch.cuh"
 #include "th_hull.cuh"
 #include "th_internal.h"
 
@@ -220,12 +221,56 @@ CarveVariants items_from_level4()
 } // namespace
 } // namespace th
 
+namespace th
+{
+namespace
+{
+
+// Shared state of the batched form: the tagged node pool of the persistent
+// carve, the request table, and the streams the per-request stages run on.
+struct BatchState
+{
+    DevBuf reqs, nodes, node_skip, ctr;
+    BatchReq* host_reqs = nullptr; // pinned
+    int32_t host_reqs_cap = 0;
+    BatchCounters* host_ctr = nullptr; // pinned
+    int64_t node_cap = 0;
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> joins;
+    cudaEvent_t fork = nullptr;
+
+    void release()
+    {
+        for (DevBuf* b : { &reqs, &nodes, &node_skip, &ctr })
+            b->release();
+        if (host_reqs)
+            cudaFreeHost(host_reqs);
+        if (host_ctr)
+            cudaFreeHost(host_ctr);
+        host_reqs = nullptr;
+        host_ctr = nullptr;
+        for (auto s : streams)
+            cudaStreamDestroy(s);
+        for (auto e : joins)
+            cudaEventDestroy(e);
+        if (fork)
+            cudaEventDestroy(fork);
+        streams.clear();
+        joins.clear();
+        fork = nullptr;
+    }
+};
+
+} // namespace
+} // namespace th
+
 struct th_context
 {
     int device = 0;
     std::string error;
     th::HullSlot hull;
     std::vector<th::HullSlot> batch;
+    th::BatchState bstate;
     th::DevBuf blur_scratch;
     bool profiling = false;
     th::StageEvents events;
@@ -298,7 +343,9 @@ int64_t max_nodes(int level)
 }
 
 // Sizes the pools of slot s for request a and fills its plan.
-void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st)
+// batch_slot: the request is part of a batch, whose octree lives in the
+// batch's shared node pool, so the slot keeps no octree pools of its own.
+void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool batch_slot = false)
 {
     const int L = a->level;
     const int64_t B = a->batch, H = a->height, W = a->width;
@@ -308,13 +355,17 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st)
     {
         // 16 M nodes and corners (about 0.5 GB) cover a level-9 hull of 32
         // megapixel views without a rerun; the pools grow x4 beyond that.
-        s.node_cap = std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 24);
-        s.corner_cap = std::min<int64_t>(R * R * R, int64_t{ 1 } << 24);
-        s.parent_cap = std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 22);
+        // Batch slots start at 4 M corners.
+        s.node_cap = batch_slot ? 1 : std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 24);
+        s.corner_cap = std::min<int64_t>(R * R * R, int64_t{ 1 } << (batch_slot ? 22 : 24));
+        s.parent_cap = batch_slot ? 1 : std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 22);
     }
-    s.node_cap = std::max<int64_t>(s.node_cap, std::min<int64_t>(max_nodes(L), 4096));
+    if (!batch_slot)
+    {
+        s.node_cap = std::max<int64_t>(s.node_cap, std::min<int64_t>(max_nodes(L), 4096));
+        s.parent_cap = std::max<int64_t>(s.parent_cap, std::min<int64_t>(max_nodes(L), 4096));
+    }
     s.corner_cap = std::max<int64_t>(s.corner_cap, std::min<int64_t>(R * R * R, 4096));
-    s.parent_cap = std::max<int64_t>(s.parent_cap, std::min<int64_t>(max_nodes(L), 4096));
     const int64_t node_cap = std::min<int64_t>(s.node_cap, max_nodes(L));
     const int64_t corner_cap = std::min<int64_t>(s.corner_cap, R * R * R);
     const int64_t parent_cap = std::min<int64_t>(s.parent_cap, node_cap);
@@ -552,6 +603,182 @@ void run_hull(th_context* ctx, HullSlot& s, const th_hull_args* a, cudaStream_t 
     ctx->carve_tuned[key] = (t_items < t_views) ? items_from_level4() : views_everywhere();
 }
 
+// Batched form: every request's SAT, then one persistent carve over all
+// octrees, one launch marking all leaves' corners, then the per-request
+// stages spread over a few streams; one device->host read at the end.
+void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_t st, th_hull_info* infos)
+{
+    for (int32_t r = 0; r < n; ++r)
+        validate(&args[r]);
+    if (n == 0)
+        return;
+    BatchState& bs = ctx->bstate;
+    if (static_cast<int32_t>(ctx->batch.size()) < n)
+        ctx->batch.resize(n);
+    const int nstreams = std::min<int32_t>(n, 8);
+    while (static_cast<int>(bs.streams.size()) < nstreams)
+    {
+        cudaStream_t s = nullptr;
+        cudaEvent_t e = nullptr;
+        TH_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        TH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        bs.streams.push_back(s);
+        bs.joins.push_back(e);
+    }
+    if (!bs.fork)
+        TH_CUDA(cudaEventCreateWithFlags(&bs.fork, cudaEventDisableTiming));
+    if (bs.host_reqs_cap < n)
+    {
+        if (bs.host_reqs)
+            TH_CUDA(cudaFreeHost(bs.host_reqs));
+        TH_CUDA(cudaMallocHost(&bs.host_reqs, sizeof(BatchReq) * n));
+        bs.host_reqs_cap = n;
+    }
+    if (!bs.host_ctr)
+        TH_CUDA(cudaMallocHost(&bs.host_ctr, sizeof(BatchCounters)));
+    int max_level = 0;
+    int64_t want_nodes = 0;
+    for (int32_t r = 0; r < n; ++r)
+    {
+        max_level = std::max(max_level, args[r].level);
+        want_nodes += std::min<int64_t>(max_nodes(args[r].level), int64_t{ 1 } << 24);
+    }
+    if (bs.node_cap == 0)
+        bs.node_cap = std::min<int64_t>(want_nodes, int64_t{ 1 } << 26);
+    bs.node_cap = std::max<int64_t>(bs.node_cap, n);
+
+    for (int32_t r = 0; r < n; ++r)
+    {
+        HullSlot& s = ctx->batch[r];
+        if (s.dirty)
+        {
+            TH_CUDA(cudaStreamWaitEvent(st, s.done, 0));
+            launch_cleanup(s.plan, st);
+            s.dirty = false;
+        }
+        s.has_result = false;
+    }
+    for (int attempt = 0; attempt < 8; ++attempt)
+    {
+        bs.reqs.ensure(sizeof(BatchReq) * n);
+        bs.nodes.ensure(sizeof(int64_t) * bs.node_cap);
+        bs.node_skip.ensure(sizeof(uint32_t) * bs.node_cap);
+        bs.ctr.ensure(sizeof(BatchCounters));
+        for (int32_t r = 0; r < n; ++r)
+        {
+            const th_hull_args* a = &args[r];
+            HullSlot& s = ctx->batch[r];
+            prepare(s, a, st, true);
+            if (attempt == 0)
+            {
+                launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), st);
+                TH_CUDA(cudaMemsetAsync(s.flags.p, 0, sizeof(unsigned int), st));
+                launch_integral_image(a->masks, a->masks_dtype, a->batch, a->height, a->width, s.sat.as<float>(), st,
+                                      s.flags.as<unsigned int>());
+            }
+            TH_CUDA(cudaMemsetAsync(s.plan.ctr, 0, sizeof(DevCounters), st));
+            const HullPlan& p = s.plan;
+            BatchReq& q = bs.host_reqs[r];
+            q = BatchReq{};
+            q.tf = p.tf;
+            q.sat = p.sat;
+            q.H = p.H;
+            q.W = p.W;
+            q.B = static_cast<int32_t>(p.B);
+            q.level = p.level;
+            q.partial = p.partial ? 1 : 0;
+            q.opengl = p.opengl ? 1 : 0;
+            q.skip_ok = p.skip_ok ? 1 : 0;
+            // empty images or no views: the octree stops at the root (see run_hull_once)
+            q.no_carve = (p.B > 0 && p.H > 0 && p.W > 0) ? 0 : 1;
+            q.nonbinary = p.nonbinary;
+            q.corner[0] = p.corner[0];
+            q.corner[1] = p.corner[1];
+            q.corner[2] = p.corner[2];
+            q.length = p.length;
+            q.bitmap = p.bitmap;
+            q.rowbits = p.rowbits;
+            q.R = p.R;
+            q.WR = p.WR;
+        }
+        TH_CUDA(cudaMemcpyAsync(bs.reqs.p, bs.host_reqs, sizeof(BatchReq) * n, cudaMemcpyHostToDevice, st));
+        BatchPlan bp{};
+        bp.reqs = bs.reqs.as<BatchReq>();
+        bp.nreq = n;
+        bp.max_level = max_level;
+        bp.nodes = bs.nodes.as<int64_t>();
+        bp.node_skip = bs.node_skip.as<uint32_t>();
+        bp.node_cap = bs.node_cap;
+        bp.ctr = bs.ctr.as<BatchCounters>();
+        launch_batch_init(bp, st);
+        launch_batch_carve(bp, st);
+        launch_batch_mark(bp, st);
+        // per-request stages, spread over the streams
+        TH_CUDA(cudaEventRecord(bs.fork, st));
+        for (int i = 0; i < nstreams; ++i)
+            TH_CUDA(cudaStreamWaitEvent(bs.streams[i], bs.fork, 0));
+        for (int32_t r = 0; r < n; ++r)
+        {
+            const HullPlan& p = ctx->batch[r].plan;
+            cudaStream_t sr = bs.streams[r % nstreams];
+            launch_rank_corners(p, sr);
+            launch_field(p, sr);
+            launch_marching_cubes(p, sr);
+        }
+        for (int i = 0; i < nstreams; ++i)
+        {
+            TH_CUDA(cudaEventRecord(bs.joins[i], bs.streams[i]));
+            TH_CUDA(cudaStreamWaitEvent(st, bs.joins[i], 0));
+        }
+        TH_CUDA(cudaMemcpyAsync(bs.host_ctr, bp.ctr, sizeof(BatchCounters), cudaMemcpyDeviceToHost, st));
+        for (int32_t r = 0; r < n; ++r)
+            TH_CUDA(cudaMemcpyAsync(ctx->batch[r].host, ctx->batch[r].plan.ctr, sizeof(DevCounters),
+                                    cudaMemcpyDeviceToHost, st));
+        TH_CUDA(cudaStreamSynchronize(st));
+        bool retry = false;
+        if (bs.host_ctr->overflow)
+        {
+            bs.node_cap *= 4;
+            retry = true;
+        }
+        for (int32_t r = 0; r < n; ++r)
+        {
+            HullSlot& s = ctx->batch[r];
+            s.dirty = true;
+            if (s.host->overflow & kOverflowCorners)
+            {
+                s.corner_cap *= 4;
+                retry = true;
+            }
+        }
+        if (!retry)
+            break;
+        for (int32_t r = 0; r < n; ++r)
+        {
+            launch_cleanup(ctx->batch[r].plan, st);
+            ctx->batch[r].dirty = false;
+        }
+        if (attempt == 7)
+            throw ArgError{ TH_ERR_OUT_OF_MEMORY, "batch pools could not be grown enough" };
+    }
+    for (int32_t r = 0; r < n; ++r)
+    {
+        HullSlot& s = ctx->batch[r];
+        const DevCounters& c = *s.host;
+        th_hull_info info{};
+        info.num_corners = c.corners;
+        info.num_levels = 0; // per-level candidates are not kept by the batched form
+        if (c.soup > 0)
+        {
+            info.num_verts = s.plan.unique ? c.verts : c.soup;
+            info.num_faces = c.soup / 3;
+        }
+        s.info = info;
+        s.has_result = true;
+        infos[r] = info;
+    }
+}
+
 th_status fail(th_context* ctx, th_status st, const std::string& msg)
 {
     if (ctx)
@@ -621,6 +848,7 @@ void th_context_destroy(th_context* ctx)
     for (auto& s : ctx->batch)
         s.release();
     ctx->blur_scratch.release();
+    ctx->bstate.release();
     ctx->events.destroy();
     for (auto& e : ctx->tune_ev)
         if (e)
@@ -831,14 +1059,7 @@ th_status th_visual_hull_batch(th_context* ctx, const th_hull_args* args, int32_
     return guarded(ctx, [&] {
         if (n < 0 || (n > 0 && (!args || !infos)))
             throw ArgError{ TH_ERR_INVALID_ARGUMENT, "invalid batch arguments" };
-        if (static_cast<int32_t>(ctx->batch.size()) < n)
-            ctx->batch.resize(n);
-        auto st = static_cast<cudaStream_t>(stream);
-        for (int32_t i = 0; i < n; ++i)
-        {
-            run_hull(ctx, ctx->batch[i], &args[i], st, nullptr);
-            infos[i] = ctx->batch[i].info;
-        }
+        run_batch(ctx, args, n, static_cast<cudaStream_t>(stream), infos);
     });
 }
 

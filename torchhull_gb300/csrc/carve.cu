@@ -52,6 +52,7 @@
 
 #include <cfloat>
 
+#include "th_classify.cuh"
 #include "th_hull.cuh"
 #include "th_internal.h"
 
@@ -134,10 +135,11 @@ __global__ void __launch_bounds__(32 * kWarps) classify_views_kernel(HullPlan p,
         if (valid)
         {
             float wx[3], wy[3], wz[3];
-            lattice_world(p, L.parents[pi], li, L.inv_rc, wx, wy, wz);
+            lattice_world(p.corner, p.length, L.parents[pi], li, L.inv_rc, wx, wy, wz);
+            const ViewSource src{ p.tf, p.sat, p.H, p.W };
             for (int64_t b = sub; b < p.B; b += LANES)
             {
-                const ItemResult r = classify_item<PARTIAL, OPENGL>(p, b, wx, wy, wz, produce, L.skip_inside);
+                const ItemResult r = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, produce, L.skip_inside);
                 empty |= r.empty;
                 refine |= r.refine;
                 inside |= r.inside;
@@ -169,35 +171,6 @@ __global__ void __launch_bounds__(32 * kWarps) classify_views_kernel(HullPlan p,
             }
         }
     }
-}
-
-struct WarpSlots
-{
-    uint32_t empty[32], refine[32], inside[32];
-    uint32_t cskip[32][8];
-};
-
-// Position of the j-th set bit of m (j < popc(m)).
-__device__ __forceinline__ int select_bit(uint32_t m, int j)
-{
-    for (int t = 0; t < j; ++t)
-        m &= m - 1;
-    return __ffs(m) - 1;
-}
-
-// OR of v over the run of lanes with the same slot s (slots ascend over the
-// lanes); the run's first lane returns the full OR.
-__device__ __forceinline__ uint32_t run_or(uint32_t v, int s, int lane)
-{
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1)
-    {
-        const uint32_t vo = __shfl_down_sync(0xffffffffu, v, d);
-        const int so = __shfl_down_sync(0xffffffffu, s, d);
-        if (lane + d < 32 && so == s)
-            v |= vo;
-    }
-    return v;
 }
 
 // (parent, view) items: a warp deals the unskipped views of a chunk of parents
@@ -261,8 +234,9 @@ __global__ void __launch_bounds__(32 * kWarps) classify_items_kernel(HullPlan p,
                 const int na = __popc(active);
                 b = j < na ? select_bit(active, j) : 32 + (j - na);
                 float wx[3], wy[3], wz[3];
-                lattice_world(p, is, li, L.inv_rc, wx, wy, wz);
-                res = classify_item<PARTIAL, OPENGL>(p, b, wx, wy, wz, L.produce && b < 32, L.skip_inside);
+                lattice_world(p.corner, p.length, is, li, L.inv_rc, wx, wy, wz);
+                const ViewSource src{ p.tf, p.sat, p.H, p.W };
+                res = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, L.produce && b < 32, L.skip_inside);
             }
             const int seg = act ? s : -1 - lane;
             const int prev_seg = __shfl_up_sync(0xffffffffu, seg, 1);

@@ -68,12 +68,6 @@ __device__ __forceinline__ bool corner_rank(const HullPlan& p, int64_t x, int64_
     return true;
 }
 
-__device__ __forceinline__ void set_bits(uint64_t* words, int64_t w, uint64_t bits)
-{
-    if ((words[w] & bits) != bits)
-        atomicOr(reinterpret_cast<unsigned long long*>(words + w), static_cast<unsigned long long>(bits));
-}
-
 __global__ void __launch_bounds__(256) mark_corners_kernel(HullPlan p)
 {
     const DevCounters* c = p.ctr;
@@ -85,24 +79,8 @@ __global__ void __launch_bounds__(256) mark_corners_kernel(HullPlan p)
     for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
     {
         const int64_t idx = leaves[t];
-        const int64_t x = idx % r, y = idx / r % r, z = idx / (r * r);
-        const int b = static_cast<int>(x & 63);
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-        {
-            const int64_t row = (y + (q & 1)) + (z + (q >> 1)) * p.R;
-            const int64_t w = row * p.WR + (x >> 6);
-            if (b < 63)
-                set_bits(p.bitmap, w, 3ull << b);
-            else
-            {
-                set_bits(p.bitmap, w, 1ull << 63);
-                set_bits(p.bitmap, w + 1, 1ull);
-            }
-            const uint32_t rb = 1u << (row & 31);
-            if (!(p.rowbits[row >> 5] & rb))
-                atomicOr(p.rowbits + (row >> 5), rb);
-        }
+        const int64_t x = idx & (r - 1), y = (idx >> L) & (r - 1), z = idx >> (2 * L);
+        mark_cell_corners(p.bitmap, p.rowbits, p.R, p.WR, x, y, z);
     }
 }
 
@@ -510,6 +488,11 @@ void launch_corners(const HullPlan& p, cudaStream_t s)
     const int64_t max_leaves = p.node_cap;
     mark_corners_kernel<<<grid_for(max_leaves, 256), 256, 0, s>>>(p);
     TH_LAUNCH_CHECK();
+    launch_rank_corners(p, s);
+}
+
+void launch_rank_corners(const HullPlan& p, cudaStream_t s)
+{
     const int64_t row_words = (p.R * p.R + 31) / 32;
     run_scan(RowCount{ p.rowbits }, RowEmit{ p.rowbits, p.rows }, RowEpilogue{ p.ctr }, Count{ nullptr, row_words },
              row_words, p.tile_sums, &p.ctr->scan, s);

@@ -1,0 +1,58 @@
+// Batched form: many hull requests carved by one persistent launch.
+#pragma once
+
+#include <cstdint>
+
+#include "th_common.cuh"
+
+namespace th
+{
+
+// Device descriptor of one request of a batch.
+struct BatchReq
+{
+    const float* tf;  // [B,16]
+    const float* sat; // [B,H,W]
+    int64_t H, W;
+    int32_t B, level;
+    int32_t partial, opengl;
+    int32_t skip_ok;  // exact integer SAT sums (size); binary masks are checked on the device
+    int32_t no_carve; // no views or an empty image: the root is refined no further
+    const unsigned int* nonbinary;
+    float corner[3];
+    float length;
+    // corner bitmap of this request (R points per axis, WR words per row)
+    uint64_t* bitmap;
+    uint32_t* rowbits;
+    int64_t R, WR;
+};
+
+struct BatchCounters
+{
+    int64_t count[kMaxLevel + 2];            // entries of level i (all requests)
+    unsigned long long head[kMaxLevel + 2];  // dequeue position of level i
+    unsigned long long overflow;
+};
+
+// Entries: request index in bits 40.., the cell (ravelled at resolution 2^i,
+// i the level of the list holding it) in bits 0..39.
+constexpr int kTagShift = 40;
+
+struct BatchPlan
+{
+    const BatchReq* reqs;
+    int32_t nreq;
+    int32_t max_level;
+    int64_t* nodes; // level lists back to back (level i starts after levels < i)
+    uint32_t* node_skip;
+    int64_t node_cap;
+    BatchCounters* ctr;
+};
+
+void launch_batch_init(const BatchPlan& bp, cudaStream_t s);
+// The whole octree of every request, in one cooperative launch.
+void launch_batch_carve(const BatchPlan& bp, cudaStream_t s);
+// Corner bits of every request's leaves, in one launch.
+void launch_batch_mark(const BatchPlan& bp, cudaStream_t s);
+
+} // namespace th

@@ -130,6 +130,50 @@ struct ItemResult
     uint32_t empty, refine, inside, skip; // 8-bit child masks
 };
 
+// Shared-memory accumulators of one warp's chunk of parents (one slot each).
+struct WarpSlots
+{
+    uint32_t empty[32], refine[32], inside[32];
+    uint32_t cskip[32][8];
+};
+
+// Position of the j-th set bit of m (j < popc(m)).
+__device__ __forceinline__ int select_bit(uint32_t m, int j)
+{
+    for (int t = 0; t < j; ++t)
+        m &= m - 1;
+    return __ffs(m) - 1;
+}
+
+// OR of v over the run of lanes with the same slot s (slots ascend over the
+// lanes); the run's first lane returns the full OR.
+__device__ __forceinline__ uint32_t run_or(uint32_t v, int s, int lane)
+{
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1)
+    {
+        const uint32_t vo = __shfl_down_sync(0xffffffffu, v, d);
+        const int so = __shfl_down_sync(0xffffffffu, s, d);
+        if (lane + d < 32 && so == s)
+            v |= vo;
+    }
+    return v;
+}
+
+// Slot owning item k: the last lane whose exclusive item offset is <= k.
+__device__ __forceinline__ int item_slot(int excl, int k)
+{
+    int s = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1)
+    {
+        const int e = __shfl_sync(0xffffffffu, excl, s + step);
+        if (s + step < 32 && e <= k)
+            s += step;
+    }
+    return s;
+}
+
 // World coordinates of the lattice of the cell idx (ravelled at resolution
 // 2^li): c + v/r * L with the product fused (visual_hull_cuda.cu:206-213);
 // v/r == v * (1/r) exactly (r = 2^k).

@@ -100,6 +100,31 @@ void launch_hull_init(const HullPlan& p, cudaStream_t s);
 void launch_export_field(const HullPlan& p, int64_t n, int64_t* indices, float* values, cudaStream_t s);
 void launch_carve_level(const HullPlan& p, int level_index, cudaStream_t s);
 void launch_corners(const HullPlan& p, cudaStream_t s);
+// The part of launch_corners after the bitmap is set: touched rows, sorted
+// unique corners and per-word ranks.
+void launch_rank_corners(const HullPlan& p, cudaStream_t s);
+
+// Sets the 8 corner bits of a leaf cell (x, y, z) at resolution 2^L in a
+// corner bitmap of R points per axis and WR words per row.
+__device__ __forceinline__ void mark_cell_corners(uint64_t* bitmap, uint32_t* rowbits, int64_t R, int64_t WR,
+                                                  int64_t x, int64_t y, int64_t z)
+{
+    const int b = static_cast<int>(x & 63);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+    {
+        const int64_t row = (y + (q & 1)) + (z + (q >> 1)) * R;
+        const int64_t w = row * WR + (x >> 6);
+        const uint64_t bits0 = (b < 63) ? (3ull << b) : (1ull << 63);
+        if ((bitmap[w] & bits0) != bits0)
+            atomicOr(reinterpret_cast<unsigned long long*>(bitmap + w), static_cast<unsigned long long>(bits0));
+        if (b == 63 && !(bitmap[w + 1] & 1ull))
+            atomicOr(reinterpret_cast<unsigned long long*>(bitmap + w + 1), 1ull);
+        const uint32_t rb = 1u << (row & 31);
+        if (!(rowbits[row >> 5] & rb))
+            atomicOr(rowbits + (row >> 5), rb);
+    }
+}
 void launch_field(const HullPlan& p, cudaStream_t s);
 void launch_marching_cubes(const HullPlan& p, cudaStream_t s);
 void launch_export(const HullPlan& p, float* verts, int64_t* faces, cudaStream_t s);

@@ -315,6 +315,63 @@ int64_t launch_count()
     return th_launch_count();
 }
 
+// Batched form: a list of requests, each (masks, transforms, level,
+// cube_corner_bfl, cube_length, masks_partial, transforms_convention,
+// unique_verts), computed together on the device's context; returns the list
+// of (verts, faces).  All masks must be on one device.
+std::vector<std::tuple<at::Tensor, at::Tensor>> visual_hull_batch(const pybind11::list& requests)
+{
+    const int64_t n = static_cast<int64_t>(requests.size());
+    std::vector<std::tuple<at::Tensor, at::Tensor>> out;
+    if (n == 0)
+        return out;
+    std::vector<at::Tensor> keep;
+    std::vector<th_hull_args> args;
+    keep.reserve(2 * n);
+    args.reserve(n);
+    int device = -1;
+    for (const auto& item : requests)
+    {
+        auto t = item.cast<pybind11::tuple>();
+        TORCH_CHECK(t.size() == 8, "each request is (masks, transforms, level, cube_corner_bfl, cube_length, "
+                                   "masks_partial, transforms_convention, unique_verts)");
+        at::Tensor masks = t[0].cast<at::Tensor>();
+        at::Tensor transforms = t[1].cast<at::Tensor>();
+        require_cuda(masks);
+        if (device < 0)
+            device = masks.device().index();
+        TORCH_CHECK(masks.device().index() == device, "all requests of a batch must be on one device");
+        masks = masks.contiguous();
+        transforms = transforms.contiguous();
+        keep.push_back(masks);
+        keep.push_back(transforms);
+        args.push_back(hull_args(masks, transforms, t[2].cast<int>(), t[3].cast<std::array<float, 3>>(),
+                                 t[4].cast<float>(), t[5].cast<bool>(), t[6].cast<std::string>(), t[7].cast<bool>()));
+    }
+    at::cuda::CUDAGuard guard(keep[0].device());
+    DeviceContext& dc = context_for(device);
+    std::lock_guard<std::mutex> g(dc.lock);
+    void* stream = stream_of(keep[0]);
+    std::vector<th_hull_info> infos(n);
+    th_status st;
+    {
+        pybind11::gil_scoped_release nogil;
+        st = th_visual_hull_batch(dc.ctx, args.data(), static_cast<int32_t>(n), stream, infos.data());
+    }
+    check(st, dc.ctx);
+    const auto opts = at::TensorOptions().device(keep[0].device());
+    for (int64_t i = 0; i < n; ++i)
+    {
+        at::Tensor v = at::empty({ infos[i].num_verts, 3 }, opts.dtype(at::kFloat));
+        at::Tensor f = at::empty({ infos[i].num_faces, 3 }, opts.dtype(at::kLong));
+        check(th_visual_hull_batch_export(dc.ctx, static_cast<int32_t>(i), v.data_ptr<float>(), f.data_ptr<int64_t>(),
+                                          stream),
+              dc.ctx);
+        out.emplace_back(v, f);
+    }
+    return out;
+}
+
 // TH_OPTION_CARVE_KERNEL: 0 autotune, 1 views over lanes, 2 (parent, view) items.
 void set_carve_kernel(int device, int mode)
 {
@@ -407,6 +464,9 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
     m.def("set_profiling", &set_profiling, "device"_a, "enable"_a, "Record CUDA events between hull stages.");
     m.def("stage_times", &stage_times, "device"_a, "Stage times (ms) of the last profiled visual_hull call.");
     m.def("launch_count", &launch_count, "Kernels launched by the CUDA library in this process.");
+    m.def("visual_hull_batch", &visual_hull_batch, "requests"_a,
+          "Batched visual hulls: list of (masks, transforms, level, cube_corner_bfl, cube_length, masks_partial, "
+          "transforms_convention, unique_verts) -> list of (verts, faces).");
     m.def("set_carve_kernel", &set_carve_kernel, "device"_a, "mode"_a,
           "Carve kernel choice: 0 autotune, 1 views over lanes, 2 (parent, view) items.");
     pybind11::class_<HullContext>(m, "HullContext", "Context with its own device pools (one request at a time).")
