@@ -1,22 +1,32 @@
 """Benchmark of the visual-hull path: hulls/s on the level-9, 32x1024^2 partial-view workload.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--mode headline|hetero|serve]
 
-Workload (one "step"): the visual hull of Q requests (default 4), each a
-distinct seeded scene of 8 ellipsoids + 20 thin capsules seen by 32 cameras at
-radius 1.4 (fov 50 deg, OpenGL convention) as float32 masks [32,1024,1024,1],
-masks_partial=True, level 9, unique vertices.  The masks are synthetic (ray
-tests at pixel centres) and stand in for the reference's OpenGL-rendered
-dataset.  Each request's masks are 128 MiB, so inputs exceed L2 between
-timed iterations.
+Headline workload (one "step"): the visual hulls of Q requests (default 4),
+each a distinct seeded scene of 8 ellipsoids + 20 thin capsules seen by 32
+cameras at radius 1.4 (fov 50 deg, OpenGL convention) as float32 masks
+[32,1024,1024,1], masks_partial=True, level 9, unique vertices.  The masks are
+synthetic (ray tests at pixel centres) and stand in for the reference's
+OpenGL-rendered dataset.  Each request's masks are 128 MiB, so the inputs
+exceed L2 between timed iterations.
 
-GB300 arm: inputs resident in HBM; every hull goes through the public
-drop-in (torchhull_gb300.visual_hull, i.e. the C ABI).  `value` is hulls/s
-of the whole job, `e2e` the same metric with the masks copied from pinned
-host memory and the mesh copied back inside the timed region.  Stage times
-come from CUDA events the library records between stages on the request's
-stream; the largest stage is the roofline line.  Under torchrun every rank
-serves its own requests (weak scaling, no collective on the data path).
+GB300 arm: inputs resident in HBM.  `value` is hulls/s of the batched form
+(all Q requests of a step in one th_visual_hull_batch call: one persistent
+carve launch over the Q octrees).  Beside it: the plain drop-in
+(torchhull_gb300.visual_hull, one request per call) as hulls/s and p50/p99
+per hull, stage times from CUDA events the library records between stages on
+the request's stream (the largest stage is the roofline line), and `e2e`: the
+batched step with the masks copied in from pinned host memory and the meshes
+copied back inside the timed region.  Under torchrun every rank serves its own
+requests (weak scaling, no collective on the data path).
+
+--mode hetero: 64 heterogeneous requests (views U{4..48}, side
+U{256,512,768,1024}, level U{6..9}, partial ~ Bernoulli(0.3)), batched vs plain.
+--mode serve: Poisson arrivals (default 200/s for 20 s) from a pool of
+pregenerated requests of the heterogeneous distribution plus 2 % large ones
+(64 views of 2048^2, level 10) through the continuous-batching server (60 GB
+admission budget), against the same stream served one request at a time.
 
 Reference arm: the reference has no CPU path and its CUDA build cannot be
 built here, so it times the CPU restatement of the reference's algorithm
@@ -42,7 +52,9 @@ sys.path.insert(0, str(ROOT))
 LEVEL = 9
 VIEWS = 32
 SIDE = 1024
-METRIC = "hulls/s, level 9, 32x1024^2 views, partial masks (p50/p99 ms per hull alongside)"
+METRIC = "hulls/s, level 9, 32x1024^2 views, partial masks (batched form; plain p50/p99 ms per hull alongside)"
+WORKLOAD = ("partial-view visual hull: 32 views of 1024x1024 float32 masks, level 9, masks_partial=True, "
+            "unique_verts=True, OpenGL, 8 ellipsoids + 20 capsules")
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 
 
@@ -127,6 +139,83 @@ def algorithmic_bytes(info_levels: list[int], corners: int, verts: int, faces: i
     return out
 
 
+def as_tuple(r):
+    return (r.masks, r.transforms, r.level, r.cube_corner_bfl, r.cube_length, r.masks_partial,
+            r.transforms_convention, r.unique_verts)
+
+
+def percentile(sorted_vals: list[float], p: float) -> float | None:
+    if not sorted_vals:
+        return None
+    return sorted_vals[min(len(sorted_vals) - 1, int(round(p / 100.0 * (len(sorted_vals) - 1))))]
+
+
+def max_over_ranks(x: float, world: int, dev) -> float:
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], device=dev, dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def timed_batches(th, tuples, steps: int, dev, world: int) -> float:
+    """Device time (ms, max over ranks) of `steps` batched calls."""
+    import torch
+    import torch.distributed as dist
+
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(steps):
+        th._C.visual_hull_batch(tuples)
+    stop.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    return max_over_ranks(start.elapsed_time(stop), world, dev)
+
+
+def timed_plain(th, reqs, steps: int, dev, world: int, local: int, profile: bool):
+    """Plain drop-in, one request per call: (ms max over ranks, per-hull ms, stage times)."""
+    import torch
+    import torch.distributed as dist
+
+    if profile:
+        th._C.set_profiling(local, True)
+    per_hull: list[float] = []
+    stages: dict[str, list] = {}
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(steps):
+        for r in reqs:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            th.visual_hull(**r.kwargs())
+            e1.record()
+            e1.synchronize()
+            per_hull.append(e0.elapsed_time(e1))
+            if profile:
+                for k, val in th._C.stage_times(local).items():
+                    stages.setdefault(k, []).append(val)
+    stop.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    if profile:
+        th._C.set_profiling(local, False)
+    return max_over_ranks(start.elapsed_time(stop), world, dev), sorted(per_hull), stages
+
+
 def run_gb300(args) -> dict | None:
     import torch
     import torch.distributed as dist
@@ -139,121 +228,87 @@ def run_gb300(args) -> dict | None:
     dev = torch.device("cuda", local)
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
-
     th._C.set_carve_kernel(local, {"auto": 0, "views": 1, "items": 2}[args.carve_kernel])
+
+    if args.mode == "hetero":
+        return finish(run_hetero(args, th, scenes, dev, world, rank), world)
+    if args.mode == "serve":
+        return finish(run_serve(args, th, scenes, dev, world, rank), world)
+
     Q = args.requests
     reqs = [scenes.partial_request(device=dev, seed=3 + 1000 * rank + q) for q in range(Q)]
+    tuples = [as_tuple(r) for r in reqs]
     torch.cuda.synchronize()
-
-    def hull(r):
-        return th.visual_hull(r.masks, r.transforms, r.level, r.cube_corner_bfl, r.cube_length, r.masks_partial,
-                              r.transforms_convention, r.unique_verts)
-
     for _ in range(args.warmup):
+        th._C.visual_hull_batch(tuples)
         for r in reqs:
-            hull(r)
+            th.visual_hull(**r.kwargs())
     torch.cuda.synchronize()
 
-    th._C.set_profiling(local, True)
-    stage_acc: dict[str, list] = {}
-    per_hull_ms: list[float] = []
-    sizes = []
+    # batched form: the value
     sampler = ClockSampler(local)
     launches0 = th._C.launch_count()
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
     sampler.start()
-    start = torch.cuda.Event(enable_timing=True)
-    stop = torch.cuda.Event(enable_timing=True)
-    start.record()
-    for _ in range(args.steps):
-        for r in reqs:
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            v, f = hull(r)
-            e1.record()
-            e1.synchronize()
-            per_hull_ms.append(e0.elapsed_time(e1))
-            st = th._C.stage_times(local)
-            for k, val in st.items():
-                stage_acc.setdefault(k, []).append(val)
-            sizes.append((v.shape[0], f.shape[0]))
-    stop.record()
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
+    batch_ms = timed_batches(th, tuples, args.steps, dev, world)
     clocks = sampler.stop()
     launches = th._C.launch_count() - launches0
-    th._C.set_profiling(local, False)
-    elapsed_ms = start.elapsed_time(stop)
-    t = torch.tensor([elapsed_ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    max_ms = float(t.item())
-    hulls = Q * args.steps * world
-    value = hulls / (max_ms / 1000.0)
+    value = Q * args.steps * world / (batch_ms / 1000.0)
 
-    # end to end: masks from pinned host memory in, mesh out, inside the timed region
+    # plain drop-in: throughput, latency, stage times
+    plain_ms, per_hull, stages = timed_plain(th, reqs, args.steps, dev, world, local, profile=True)
+    plain_value = Q * args.steps * world / (plain_ms / 1000.0)
+
+    # end to end: batched step with masks copied in from pinned host memory and meshes copied back
     host_masks = [r.masks.cpu().pin_memory() for r in reqs]
     host_tf = [r.transforms.cpu().pin_memory() for r in reqs]
     dev_masks = [torch.empty_like(r.masks) for r in reqs]
     dev_tf = [torch.empty_like(r.transforms) for r in reqs]
     h2d = sum(m.numel() * m.element_size() for m in host_masks) + sum(x.numel() * x.element_size() for x in host_tf)
-    d2h_total = 0
+    # the meshes are deterministic: pinned result buffers sized from one untimed call
+    first = th._C.visual_hull_batch(tuples)
+    host_out = [(torch.empty(v.shape, dtype=v.dtype, pin_memory=True),
+                 torch.empty(f.shape, dtype=f.dtype, pin_memory=True)) for v, f in first]
+    d2h = sum(vh.numel() * vh.element_size() + fh.numel() * fh.element_size() for vh, fh in host_out)
     e2e_steps = max(1, args.steps // 2)
+    if world > 1:
+        dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for q, r in enumerate(reqs):
+        for q in range(Q):
             dev_masks[q].copy_(host_masks[q], non_blocking=True)
             dev_tf[q].copy_(host_tf[q], non_blocking=True)
-            v, f = th.visual_hull(dev_masks[q], dev_tf[q], r.level, r.cube_corner_bfl, r.cube_length, r.masks_partial,
-                                  r.transforms_convention, r.unique_verts)
-            vh = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
-            fh = torch.empty(f.shape, dtype=f.dtype, pin_memory=True)
+        out = th._C.visual_hull_batch([(dev_masks[q], dev_tf[q]) + tuples[q][2:] for q in range(Q)])
+        for (v, f), (vh, fh) in zip(out, host_out, strict=True):
             vh.copy_(v, non_blocking=True)
             fh.copy_(f, non_blocking=True)
-            d2h_total += vh.numel() * 4 + fh.numel() * 8
         torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    t = torch.tensor([e2e_s], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_value = Q * e2e_steps * world / float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    e2e_value = Q * e2e_steps * world / e2e_s
 
     if rank != 0:
-        if world > 1:
-            dist.destroy_process_group()
-        return None
+        return finish(None, world)
 
-    # roofline from the stage events of the timed region
-    info = th.visual_hull_with_candidate_voxels(reqs[0].masks, reqs[0].transforms, LEVEL, reqs[0].cube_corner_bfl,
-                                                reqs[0].cube_length, True, "opengl", True)
+    # roofline of the dominant stage, from the stage events of the plain timed region
+    r0 = reqs[0]
+    info = th.visual_hull_with_candidate_voxels(**r0.kwargs())
     levels = [c.numel() for c in info[2]]
-    field = th.sparse_visual_hull_field(reqs[0].masks, reqs[0].transforms, LEVEL, reqs[0].cube_corner_bfl,
-                                        reqs[0].cube_length, True, "opengl")
+    field = th.sparse_visual_hull_field(r0.masks, r0.transforms, LEVEL, r0.cube_corner_bfl, r0.cube_length, True,
+                                        "opengl")
     corners = field.values().numel()
     nv, nf = info[0].shape[0], info[1].shape[0]
     algo = algorithmic_bytes(levels, corners, nv, nf, VIEWS, SIDE, SIDE, 4)
     mean = {k: (statistics.fmean(v) if not isinstance(v[0], list) else [statistics.fmean(x) for x in zip(*v)])
-            for k, v in stage_acc.items()}
-    candidates = [("integral_image", "sat_columns_kernel+sat_rows_kernel", mean["integral_image"],
-                   algo["integral_image"])]
+            for k, v in stages.items()}
+    cands = [("integral_image", "sat_columns_kernel+sat_rows_kernel", mean["integral_image"], algo["integral_image"])]
     for i, ms in enumerate(mean["carve"]):
-        candidates.append((f"carve_level_{i}", "classify_kernel+scan", ms, algo["carve"][i]))
-    candidates += [("corners", "mark_corners_kernel+scans", mean["corners"], algo["corners"]),
-                   ("field", "field_kernel", mean["field"], algo["field"]),
-                   ("marching_cubes", "mc_cells_kernel+scan", mean["marching_cubes"], algo["marching_cubes"])]
-    dom = max(candidates, key=lambda c: c[2])
+        cands.append((f"carve_level_{i}", "classify_*_kernel+scan", ms, algo["carve"][i]))
+    cands += [("corners", "mark_corners_kernel+scans", mean["corners"], algo["corners"]),
+              ("field", "field_kernel", mean["field"], algo["field"]),
+              ("marching_cubes", "mc_cells_kernel+scan", mean["marching_cubes"], algo["marching_cubes"])]
+    dom = max(cands, key=lambda c: c[2])
     peak, peak_kind = peaks()
     achieved = dom[3] / (dom[2] / 1000.0) / 1e9
-    per_hull_ms.sort()
-
-    def pct(p):
-        return per_hull_ms[min(len(per_hull_ms) - 1, int(round(p / 100.0 * (len(per_hull_ms) - 1))))]
-
     line = {
         "metric": METRIC,
         "value": value,
@@ -261,23 +316,24 @@ def run_gb300(args) -> dict | None:
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": max_ms / args.steps,
+        "ms_per_step": batch_ms / args.steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic: seeded ray-ellipsoid/capsule masks (stand-in for the reference's rendered dataset)",
-        "config": {"workload": "partial-view visual hull: 32 views of 1024x1024 float32 masks, level 9, "
-                               "masks_partial=True, unique_verts=True, OpenGL, 8 ellipsoids + 20 capsules",
-                   "requests_per_step": Q, "level": LEVEL, "views": VIEWS, "side": SIDE,
+        "config": {"workload": WORKLOAD, "requests_per_step": Q, "level": LEVEL, "views": VIEWS, "side": SIDE,
                    "l2": "inputs larger than L2 (128 MiB of masks + 128 MiB SAT per request)",
-                   "path": "plain drop-in visual_hull per request (C ABI)",
+                   "path": "batched form (th_visual_hull_batch: one persistent carve launch per step)",
                    "mesh_verts": nv, "mesh_faces": nf, "leaves": levels[-1], "corners": corners},
-        "p50_ms": pct(50),
-        "p99_ms": pct(99),
+        "plain": {"value": plain_value, "unit": "hulls/s", "p50_ms": percentile(per_hull, 50),
+                  "p99_ms": percentile(per_hull, 99), "path": "torchhull_gb300.visual_hull, one request per call"},
+        "batched_over_plain": value / plain_value,
+        "p50_ms": percentile(per_hull, 50),
+        "p99_ms": percentile(per_hull, 99),
         "stage_ms": mean,
         "e2e": {"value": e2e_value, "unit": "hulls/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h_total // e2e_steps},
+                "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": dom[1], "stage": dom[0], "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes": dom[3], "ms": dom[2], "traffic": None},
@@ -286,9 +342,101 @@ def run_gb300(args) -> dict | None:
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(reqs[0], samples=args.cpu_samples)
+    return finish(line, world)
+
+
+def finish(line, world):
     if world > 1:
+        import torch.distributed as dist
+
         dist.destroy_process_group()
     return line
+
+
+def run_hetero(args, th, scenes, dev, world, rank):
+    import torch
+
+    reqs = scenes.batched_requests(count=args.hetero_count, seed=4 + 1000 * rank, device=dev)
+    tuples = [as_tuple(r) for r in reqs]
+    for _ in range(max(1, args.warmup)):
+        th._C.visual_hull_batch(tuples)
+        for r in reqs:
+            th.visual_hull(**r.kwargs())
+    torch.cuda.synchronize()
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    launches0 = th._C.launch_count()
+    batch_ms = timed_batches(th, tuples, args.steps, dev, world)
+    launches = th._C.launch_count() - launches0
+    clocks = sampler.stop()
+    plain_ms, per_hull, _ = timed_plain(th, reqs, args.steps, dev, world, dev.index or 0, profile=False)
+    n = len(reqs)
+    if rank != 0:
+        return None
+    value = n * args.steps * world / (batch_ms / 1000.0)
+    plain_value = n * args.steps * world / (plain_ms / 1000.0)
+    return {
+        "metric": "hulls/s, 64 heterogeneous requests (batched form)", "value": value, "unit": "hulls/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded ray-ellipsoid/capsule masks",
+        "config": {"workload": "64 requests: views U{4..48}, side U{256,512,768,1024}, level U{6..9}, "
+                               "masks_partial ~ Bernoulli(0.3), float32", "requests_per_step": n},
+        "plain": {"value": plain_value, "unit": "hulls/s", "p50_ms": percentile(per_hull, 50),
+                  "p99_ms": percentile(per_hull, 99)},
+        "batched_over_plain": value / plain_value,
+        "clocks": clocks, "gpu_launches": launches,
+    }
+
+
+def run_serve(args, th, scenes, dev, world, rank):
+    import numpy as np
+    import torch
+
+    from torchhull_gb300.serve import HullServer
+
+    pool = scenes.batched_requests(count=args.serve_pool, seed=6 + 1000 * rank, device=dev)
+    large = [scenes.make_request(9000 + 1000 * rank + i, 64, 2048, 10, False, device=dev)
+             for i in range(args.serve_large)]
+    rng = np.random.default_rng(7 + rank)
+    n = int(args.rate * args.duration)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=n))
+    picks = [large[i % len(large)] if (large and rng.random() < 0.02) else pool[int(rng.integers(len(pool)))]
+             for i in range(n)]
+    for r in pool + large:  # warm the pools and the autotuner
+        th.visual_hull(**r.kwargs())
+    torch.cuda.synchronize()
+
+    def serve(slots):
+        with HullServer(device=dev.index or 0, slots=slots, budget_bytes=60e9) as server:
+            t0 = time.perf_counter()
+            futures = []
+            for t, r in zip(arrivals, picks, strict=True):
+                delay = t - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                futures.append(server.submit(r))
+            for f in futures:
+                f.result()
+            wall = time.perf_counter() - t0
+            return n / wall, server.stats()
+
+    rate_cb, stats_cb = serve(args.serve_slots)
+    rate_one, stats_one = serve(1)
+    if rank != 0:
+        return None
+    return {
+        "metric": "hulls/s and p50/p99 ms under Poisson arrivals (continuous batching)", "value": rate_cb,
+        "unit": "hulls/s", "n_gpus": world, "steps": n, "warmup": 1, "ms_per_step": 1000.0 / rate_cb,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: pregenerated pool of seeded requests replayed by the arrival stream",
+        "config": {"workload": f"Poisson arrivals {args.rate}/s for {args.duration} s; pool of {args.serve_pool} "
+                               "requests of the heterogeneous distribution + 2% large (64x2048^2, level 10)",
+                   "slots": args.serve_slots, "budget_bytes": 60e9},
+        "p50_ms": stats_cb["p50_ms"], "p99_ms": stats_cb["p99_ms"],
+        "one_at_a_time": {"value": rate_one, "p50_ms": stats_one["p50_ms"], "p99_ms": stats_one["p99_ms"]},
+        "served_over_one_at_a_time": rate_cb / rate_one,
+    }
 
 
 def octant_args(o: int):
@@ -328,13 +476,10 @@ def run_reference(args) -> dict | None:
     for w in range(args.warmup):
         corner, length, level = octant_args(w % 8)
         oracle.visual_hull(masks, tf, level, corner, length, True, "opengl", True, nthreads=threads)
-    times = []
     t0 = time.perf_counter()
     for k in range(args.steps):
         corner, length, level = octant_args(k % 8)
-        s = time.perf_counter()
         oracle.visual_hull(masks, tf, level, corner, length, True, "opengl", True, nthreads=threads)
-        times.append(time.perf_counter() - s)
     total = time.perf_counter() - t0
     value = (args.steps / 8.0) / total
     sample = (f"each step one octant of the cube at the same leaf size (level 8 over half the cube); "
@@ -353,8 +498,7 @@ def run_reference(args) -> dict | None:
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic: seeded ray-ellipsoid/capsule masks",
-        "config": {"workload": "partial-view visual hull: 32 views of 1024x1024 float32 masks, level 9, "
-                               "masks_partial=True, unique_verts=True, OpenGL, 8 ellipsoids + 20 capsules",
+        "config": {"workload": WORKLOAD,
                    "path": "CPU restatement of the reference algorithm (the reference has no CPU path and its "
                            "CUDA build needs glm/stdgpu/charonload, absent offline)"},
         "cpu_baseline": {"value": value, "unit": "hulls/s", "cores": threads, "kind": "port", "sample": sample},
@@ -368,11 +512,18 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--mode", choices=["headline", "hetero", "serve"], default="headline")
     ap.add_argument("--requests", type=int, default=4)
     ap.add_argument("--cpu-samples", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--carve-kernel", choices=["auto", "views", "items"], default="auto",
                     help="carve kernel: autotuned (default) or forced")
+    ap.add_argument("--hetero-count", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--duration", type=float, default=20.0)
+    ap.add_argument("--serve-pool", type=int, default=24)
+    ap.add_argument("--serve-large", type=int, default=1)
+    ap.add_argument("--serve-slots", type=int, default=8)
     args = ap.parse_args()
     line = run_reference(args) if args.impl == "reference" else run_gb300(args)
     if line is not None:
