@@ -23,7 +23,7 @@ requests (weak scaling, no collective on the data path).
 
 --mode hetero: 64 heterogeneous requests (views U{4..48}, side
 U{256,512,768,1024}, level U{6..9}, partial ~ Bernoulli(0.3)), batched vs plain.
---mode serve: Poisson arrivals (default 200/s for 20 s) from a pool of
+--mode serve: Poisson arrivals (default 200/s for 10 s) from a pool of
 pregenerated requests of the heterogeneous distribution plus 2 % large ones
 (64 views of 2048^2, level 10) through the continuous-batching server (60 GB
 admission budget), against the same stream served one request at a time.
@@ -520,7 +520,7 @@ def main() -> None:
                     help="carve kernel: autotuned (default) or forced")
     ap.add_argument("--hetero-count", type=int, default=64)
     ap.add_argument("--rate", type=float, default=200.0)
-    ap.add_argument("--duration", type=float, default=20.0)
+    ap.add_argument("--duration", type=float, default=10.0)
     ap.add_argument("--serve-pool", type=int, default=24)
     ap.add_argument("--serve-large", type=int, default=1)
     ap.add_argument("--serve-slots", type=int, default=8)

@@ -42,6 +42,11 @@ NVCC_FLAGS = [
 ]
 
 
+def _defines() -> list[str]:
+    """Extra preprocessor definitions from TH_NVCC_DEFINES (space-separated NAME=VALUE), for tuning builds."""
+    return [f"-D{d}" for d in os.environ.get("TH_NVCC_DEFINES", "").split() if d]
+
+
 def _nvcc() -> str:
     cuda_home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
     cand = Path(cuda_home) / "bin" / "nvcc"
@@ -64,7 +69,7 @@ def _compile(src: str) -> Path:
     out = OBJ / (Path(src).stem + ".o")
     deps = [CSRC / src] + [CSRC / h for h in HEADERS] + [PKG.parent / "include" / "torchhull_gb300.h"]
     if _stale(out, deps):
-        cmd = [_nvcc(), *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(out)]
+        cmd = [_nvcc(), *NVCC_FLAGS, *_defines(), "-c", str(CSRC / src), "-o", str(out)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -73,6 +78,13 @@ def _compile(src: str) -> Path:
 
 def build_library(verbose: bool = False) -> Path:
     OBJ.mkdir(parents=True, exist_ok=True)
+    # objects built with other definitions are stale
+    stamp = OBJ / "defines.txt"
+    defines = " ".join(_defines())
+    if not stamp.exists() or stamp.read_text() != defines:
+        for o in OBJ.glob("*.o"):
+            o.unlink()
+        stamp.write_text(defines)
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(CU_SOURCES)) as ex:
         objs = list(ex.map(_compile, CU_SOURCES))
     if _stale(LIB, objs):

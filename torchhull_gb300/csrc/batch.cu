@@ -55,7 +55,7 @@ __device__ __forceinline__ ItemResult batch_item(const BatchReq& q,
                                                  bool want_skip,
                                                  bool skip_inside)
 {
-    const ViewSource src{ q.tf, q.sat, q.H, q.W };
+    const ViewSource src = make_view_source(q.tf, q.sat, q.H, q.W);
     if (q.partial)
         return q.opengl ? classify_item<true, true>(src, b, wx, wy, wz, want_skip, skip_inside)
                         : classify_item<true, false>(src, b, wx, wy, wz, want_skip, skip_inside);
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(32 * kBatchWarps) batch_carve_kernel(BatchPlan
     {
         const int64_t n = level_entries(bp, li, start);
         const int64_t next = start + n;
-        const float inv_rc = __fdiv_rn(1.f, static_cast<float>(int64_t{ 2 } << li)); // exact: a power of two
+        const float inv_rc = __int_as_float((127 - (li + 1)) << 23); // 2^-(li + 1), exact
         const int64_t per = (n + nwarps - 1) / nwarps;
         const int ppw = static_cast<int>(per < 1 ? 1 : (per > 32 ? 32 : per));
         for (;;)

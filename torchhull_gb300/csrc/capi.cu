@@ -329,8 +329,9 @@ void validate(const th_hull_args* a)
     // Flagged/Unique/stdgpu use 32-bit indices (visual_hull_cuda.cu:716, :798)
     if (a->batch * a->height * a->width >= (int64_t{ 1 } << 40))
         throw ArgError{ TH_ERR_INVALID_ARGUMENT, "masks too large" };
-    if (a->height >= (int64_t{ 1 } << 31) || a->width >= (int64_t{ 1 } << 31))
-        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "mask height and width must be below 2^31" };
+    // pixel indices are carried exactly in float mantissas by the carve
+    if (a->height >= (int64_t{ 1 } << 23) || a->width >= (int64_t{ 1 } << 23))
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "mask height and width must be below 2^23" };
 }
 
 int64_t max_nodes(int level)

@@ -63,6 +63,11 @@ namespace
 {
 
 constexpr int kWarps = 8; // warps per block of the classify kernels
+#ifndef TH_CARVE_MIN_BLOCKS
+#define TH_CARVE_MIN_BLOCKS 2
+#endif
+// resident blocks per SM the classify kernels' register budget is cut for
+constexpr int kMinBlocks = TH_CARVE_MIN_BLOCKS;
 
 __global__ void hull_init_kernel(HullPlan p)
 {
@@ -98,7 +103,7 @@ __device__ __forceinline__ LevelInfo level_info(const HullPlan& p, int li, bool 
     const int64_t off = ctr->level_off[li];
     L.parents = p.nodes + off;
     L.parent_skip = p.node_skip + off;
-    L.inv_rc = __fdiv_rn(1.f, static_cast<float>(int64_t{ 2 } << li)); // exact: a power of two
+    L.inv_rc = __int_as_float((127 - (li + 1)) << 23); // 2^-(li + 1), exact
     L.last = (li == p.level - 1);
     L.skips = p.skip_ok && (*p.nonbinary == 0);
     // the children are parents of the next level, which uses the item kernel
@@ -117,7 +122,7 @@ __device__ __forceinline__ void store_parent(const HullPlan& p, const LevelInfo&
 
 // Views over lanes: a group of LANES lanes owns one parent.
 template <int LANES, bool PARTIAL, bool OPENGL>
-__global__ void __launch_bounds__(32 * kWarps) classify_views_kernel(HullPlan p, int li)
+__global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_views_kernel(HullPlan p, int li)
 {
     constexpr int G = 32 / LANES;
     const LevelInfo L = level_info(p, li, PARTIAL);
@@ -136,7 +141,7 @@ __global__ void __launch_bounds__(32 * kWarps) classify_views_kernel(HullPlan p,
         {
             float wx[3], wy[3], wz[3];
             lattice_world(p.corner, p.length, L.parents[pi], li, L.inv_rc, wx, wy, wz);
-            const ViewSource src{ p.tf, p.sat, p.H, p.W };
+            const ViewSource src = make_view_source(p.tf, p.sat, p.H, p.W);
             for (int64_t b = sub; b < p.B; b += LANES)
             {
                 const ItemResult r = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, produce, L.skip_inside);
@@ -176,7 +181,7 @@ __global__ void __launch_bounds__(32 * kWarps) classify_views_kernel(HullPlan p,
 // (parent, view) items: a warp deals the unskipped views of a chunk of parents
 // out to its lanes.
 template <bool PARTIAL, bool OPENGL>
-__global__ void __launch_bounds__(32 * kWarps) classify_items_kernel(HullPlan p, int li)
+__global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel(HullPlan p, int li)
 {
     __shared__ WarpSlots slots_all[kWarps];
     WarpSlots& ws = slots_all[threadIdx.x >> 5];
@@ -235,7 +240,7 @@ __global__ void __launch_bounds__(32 * kWarps) classify_items_kernel(HullPlan p,
                 b = j < na ? select_bit(active, j) : 32 + (j - na);
                 float wx[3], wy[3], wz[3];
                 lattice_world(p.corner, p.length, is, li, L.inv_rc, wx, wy, wz);
-                const ViewSource src{ p.tf, p.sat, p.H, p.W };
+                const ViewSource src = make_view_source(p.tf, p.sat, p.H, p.W);
                 res = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, L.produce && b < 32, L.skip_inside);
             }
             const int seg = act ? s : -1 - lane;

@@ -186,11 +186,14 @@ __device__ __forceinline__ float mask_sample(const HullPlan& p, int64_t b, int64
 // mask sample (image_utils.h:162-214), or exactly 1 when partial mode skips
 // the view (x * 1 == x, so multiplying by it equals skipping it).
 //
-// The reference converts the rounded pixel to int64.  This uses the
-// saturating int32 conversion (64-bit conversions run on GB300's FP64 pipe):
-// the in-image tests decide identically, and where the two values differ
-// (|coordinate| >= 2^31) all four samples are padding, for which the
-// interpolation gives the same result (0, 1 or NaN) for either weight.
+// The reference converts the rounded pixel to int64.  Near the image the
+// rounding and the conversion are done exactly with float adds (the
+// conversion instructions run on narrow pipes, the 64-bit ones on GB300's
+// FP64 pipe); far from it (|coordinate| >= 2^22, or NaN) the saturating int32
+// conversion stands in: the in-image tests decide identically, and where its
+// value differs from the int64 one (|coordinate| >= 2^31) all four samples
+// are padding, for which the interpolation gives the same result (0, 1 or
+// NaN) for either weight.
 template <int DT, bool PARTIAL>
 __device__ __forceinline__ float view_factor(const HullPlan& p, int64_t b, float wx, float wy, float wz, float Hf, float Wf)
 {
@@ -198,21 +201,27 @@ __device__ __forceinline__ float view_factor(const HullPlan& p, int64_t b, float
     float px, py;
     to_pixel(m, wx, wy, wz, p.opengl, Hf, Wf, px, py);
     const float pad = PARTIAL ? 1.f : 0.f;
-    if (PARTIAL)
+    // 1 <= round(q) < size - 1 (half away from zero) exactly when 0.5 <= q < size - 1.5
+    if (PARTIAL && !(px >= 0.5f && px < __fsub_rn(Wf, 1.5f) && py >= 0.5f && py < __fsub_rn(Hf, 1.5f)))
+        return 1.f;
+    Snapped ry, rx;
+    if (!round_small(__fadd_rn(py, -0.5f), ry))
     {
-        const int64_t qx = __float2int_rz(roundf(px)), qy = __float2int_rz(roundf(py));
-        if (!(1 <= qy && qy < p.H - 1 && 1 <= qx && qx < p.W - 1))
-            return 1.f;
+        ry.i = __float2int_rz(roundf(__fadd_rn(py, -0.5f)));
+        ry.f = __int2float_rn(ry.i);
     }
-    const int32_t yp = __float2int_rz(roundf(__fadd_rn(py, -0.5f)));
-    const int32_t xp = __float2int_rz(roundf(__fadd_rn(px, -0.5f)));
-    const int64_t y0 = yp, x0 = xp;
+    if (!round_small(__fadd_rn(px, -0.5f), rx))
+    {
+        rx.i = __float2int_rz(roundf(__fadd_rn(px, -0.5f)));
+        rx.f = __int2float_rn(rx.i);
+    }
+    const int64_t y0 = ry.i, x0 = rx.i;
     const float v00 = mask_sample<DT>(p, b, y0, x0, pad);
     const float v10 = mask_sample<DT>(p, b, y0 + 1, x0, pad);
     const float v01 = mask_sample<DT>(p, b, y0, x0 + 1, pad);
     const float v11 = mask_sample<DT>(p, b, y0 + 1, x0 + 1, pad);
-    const float ty = __fsub_rn(py, __int2float_rn(yp));
-    const float tx = __fsub_rn(px, __int2float_rn(xp));
+    const float ty = __fsub_rn(py, ry.f);
+    const float tx = __fsub_rn(px, rx.f);
     return bilerp(v00, v10, v01, v11, ty, tx);
 }
 
@@ -225,7 +234,7 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p)
     const int64_t n = p.ctr->corners;
     const int64_t R = p.R;
     const float inv_rc = __fdiv_rn(1.f, static_cast<float>(R - 1)); // exact: a power of two
-    const float Hf = static_cast<float>(p.H), Wf = static_cast<float>(p.W);
+    const float Hf = small_i2f(static_cast<int32_t>(p.H)), Wf = small_i2f(static_cast<int32_t>(p.W));
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
     {
@@ -233,9 +242,10 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p)
         int64_t gx, gy, gz;
         unpack_corner(idx, gx, gy, gz);
         // c + v/r * L fused (visual_hull_cuda.cu:444-448); v/r == v * (1/r) exactly
-        const float wx = __fmaf_rn(__fmul_rn(static_cast<float>(gx), inv_rc), p.length, p.corner[0]);
-        const float wy = __fmaf_rn(__fmul_rn(static_cast<float>(gy), inv_rc), p.length, p.corner[1]);
-        const float wz = __fmaf_rn(__fmul_rn(static_cast<float>(gz), inv_rc), p.length, p.corner[2]);
+        // corner coordinates are at most 2^12
+        const float wx = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gx)), inv_rc), p.length, p.corner[0]);
+        const float wy = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gy)), inv_rc), p.length, p.corner[1]);
+        const float wz = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gz)), inv_rc), p.length, p.corner[2]);
         float value = 1.f;
 #pragma unroll 4
         for (int64_t b = 0; b < p.B; ++b)

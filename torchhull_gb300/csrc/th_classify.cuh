@@ -61,30 +61,39 @@ struct ViewResult
 // One child in one view from its pixel box (visual_hull_cuda.cu:236-285 and
 // :365-410).  The box starts the reference's min/max from +-FLT_MAX.
 // want_skip: evaluate the skip rule (the caller checked corners in front and,
-// if needed, two pixels inside).  H, W >= 1.
+// if needed, two pixels inside).  1 <= H, W < 2^23; Hf, Wf the same as floats.
 template <bool PARTIAL>
-__device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sat_b, int32_t H, int32_t W, Box bb, bool want_skip)
+__device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sat_b, int32_t H, int32_t W, float Hf, float Wf, Box bb, bool want_skip)
 {
     const float margin = 0.5f - 0.1f; // isolevel - epsilon (visual_hull_cuda.cu:259-267)
     bb.minx = fminf(FLT_MAX, bb.minx);
     bb.miny = fminf(FLT_MAX, bb.miny);
     bb.maxx = fmaxf(-FLT_MAX, bb.maxx);
     bb.maxy = fmaxf(-FLT_MAX, bb.maxy);
-    const float fminx = roundf(__fadd_rn(bb.minx, -0.5f));
-    const float fminy = roundf(__fadd_rn(bb.miny, -0.5f));
-    const float fmaxx = roundf(__fadd_rn(bb.maxx, 0.5f));
-    const float fmaxy = roundf(__fadd_rn(bb.maxy, 0.5f));
-    const int32_t cminx = min(max(f2i32(fminx), 0), W - 1);
-    const int32_t cminy = min(max(f2i32(fminy), 0), H - 1);
-    const int32_t cmaxx = min(max(f2i32(fmaxx), 0), W - 1);
-    const int32_t cmaxy = min(max(f2i32(fmaxy), 0), H - 1);
-    const int64_t area = static_cast<int64_t>(cmaxy - cminy + 1) * static_cast<int64_t>(cmaxx - cminx + 1);
-    const float sum = box_sum(sat_b, W, cminx, cminy, cmaxx, cmaxy);
+    const float vminx = __fadd_rn(bb.minx, -0.5f);
+    const float vminy = __fadd_rn(bb.miny, -0.5f);
+    const float vmaxx = __fadd_rn(bb.maxx, 0.5f);
+    const float vmaxy = __fadd_rn(bb.maxy, 0.5f);
+    // the rounded corners clamped to the image
+    const Snapped x0 = round_clamp(vminx, __fsub_rn(Wf, 1.f));
+    const Snapped y0 = round_clamp(vminy, __fsub_rn(Hf, 1.f));
+    const Snapped x1 = round_clamp(vmaxx, __fsub_rn(Wf, 1.f));
+    const Snapped y1 = round_clamp(vmaxy, __fsub_rn(Hf, 1.f));
+    const float sum = box_sum(sat_b, W, x0.i, y0.i, x1.i, y1.i);
+    // float(area) of the int64 area: a product of two exact integers, rounded once
+    const float area_f = __fmul_rn(__fadd_rn(__fsub_rn(y1.f, y0.f), 1.f), __fadd_rn(__fsub_rn(x1.f, x0.f), 1.f));
+    // every rounded corner inside the image (the clamps were no-ops): round(v)
+    // is in [0, size - 1] exactly when v is in (-0.5, size - 0.5)
+    const float hx = __fsub_rn(Wf, 0.5f), hy = __fsub_rn(Hf, 0.5f);
+    const bool framed = vminx > -0.5f && vminx < hx && vmaxx > -0.5f && vmaxx < hx && vminy > -0.5f &&
+                        vminy < hy && vmaxy > -0.5f && vmaxy < hy;
     bool whole = true;
-    if (PARTIAL)
+    if (PARTIAL && !framed)
     {
         // full_area_bb (:377) from the unclamped rounded box, int64 arithmetic
         // wrapping like the device's; exact int64 values when int32 cannot hold them.
+        const float fminx = roundf(vminx), fminy = roundf(vminy);
+        const float fmaxx = roundf(vmaxx), fmaxy = roundf(vmaxy);
         int64_t rminx, rminy, rmaxx, rmaxy;
         if (fits_i32(fminx) && fits_i32(fminy) && fits_i32(fmaxx) && fits_i32(fmaxy))
         {
@@ -100,27 +109,25 @@ __device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sa
             rmaxx = f2i64(fmaxx);
             rmaxy = f2i64(fmaxy);
         }
+        const int64_t area = static_cast<int64_t>(y1.i - y0.i + 1) * static_cast<int64_t>(x1.i - x0.i + 1);
         const uint64_t fy = static_cast<uint64_t>(rmaxy) - static_cast<uint64_t>(rminy) + 1u;
         const uint64_t fx = static_cast<uint64_t>(rmaxx) - static_cast<uint64_t>(rminx) + 1u;
         whole = (static_cast<uint64_t>(area) == fy * fx);
     }
-    const float area_f = (area >= INT32_MIN && area <= INT32_MAX) ? __int2float_rn(static_cast<int32_t>(area))
-                                                                  : __ll2float_rn(area);
     ViewResult res{ kNone, false };
     if (sum <= 0.f + margin && whole)
         res.cls = kEmpty;
     else if (sum >= __fsub_rn(area_f, margin) && whole)
         res.cls = kObject;
-    else if (!PARTIAL || (cmaxy - cminy > 1 && cmaxx - cminx > 1))
+    else if (!PARTIAL || (y1.i - y0.i > 1 && x1.i - x0.i > 1))
         res.cls = kRefine;
-    if (want_skip && res.cls == kObject && fminx >= 1.f && fminy >= 1.f && fmaxx <= static_cast<float>(W - 2) &&
-        fmaxy <= static_cast<float>(H - 2))
+    if (want_skip && res.cls == kObject && framed && x0.i >= 1 && y0.i >= 1 && x1.i <= W - 2 && y1.i <= H - 2 &&
+        x0.i <= x1.i && y0.i <= y1.i)
     {
         // the box grown by one pixel is inside the image: all ones there?
-        const int32_t x0 = static_cast<int32_t>(fminx) - 1, y0 = static_cast<int32_t>(fminy) - 1;
-        const int32_t x1 = static_cast<int32_t>(fmaxx) + 1, y1 = static_cast<int32_t>(fmaxy) + 1;
-        const float grown = box_sum(sat_b, W, x0, y0, x1, y1);
-        res.skip = grown == static_cast<float>((y1 - y0 + 1) * (x1 - x0 + 1));
+        const int32_t gx0 = x0.i - 1, gy0 = y0.i - 1, gx1 = x1.i + 1, gy1 = y1.i + 1;
+        const float grown = box_sum(sat_b, W, gx0, gy0, gx1, gy1);
+        res.skip = grown == __fmul_rn(__fadd_rn(__fsub_rn(y1.f, y0.f), 3.f), __fadd_rn(__fsub_rn(x1.f, x0.f), 3.f));
     }
     return res;
 }
@@ -187,13 +194,15 @@ __device__ __forceinline__ void lattice_world(const float corner[3],
                                               float wz[3])
 {
     const int64_t mask = (int64_t{ 1 } << li) - 1;
-    const int64_t gx = idx & mask, gy = (idx >> li) & mask, gz = idx >> (2 * li);
+    const int32_t gx = static_cast<int32_t>(idx & mask), gy = static_cast<int32_t>((idx >> li) & mask),
+                  gz = static_cast<int32_t>(idx >> (2 * li));
 #pragma unroll
     for (int d = 0; d < 3; ++d)
     {
-        wx[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gx + d), inv_rc), length, corner[0]);
-        wy[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gy + d), inv_rc), length, corner[1]);
-        wz[d] = __fmaf_rn(__fmul_rn(static_cast<float>(2 * gz + d), inv_rc), length, corner[2]);
+        // lattice coordinates below 2^(li + 1) <= 2^14
+        wx[d] = __fmaf_rn(__fmul_rn(small_i2f(2 * gx + d), inv_rc), length, corner[0]);
+        wy[d] = __fmaf_rn(__fmul_rn(small_i2f(2 * gy + d), inv_rc), length, corner[1]);
+        wz[d] = __fmaf_rn(__fmul_rn(small_i2f(2 * gz + d), inv_rc), length, corner[2]);
     }
 }
 
@@ -202,8 +211,14 @@ struct ViewSource
 {
     const float* tf;  // [B,16] float32 transforms
     const float* sat; // [B,H,W] integral images
-    int64_t H, W;
+    int64_t H, W;     // below 2^23
+    float Hf, Wf;     // H, W as floats
 };
+
+__device__ __forceinline__ ViewSource make_view_source(const float* tf, const float* sat, int64_t H, int64_t W)
+{
+    return ViewSource{ tf, sat, H, W, small_i2f(static_cast<int32_t>(H)), small_i2f(static_cast<int32_t>(W)) };
+}
 
 // One (parent, view) item: the parent's lattice projected into view b.
 // want_skip: compute the children's skip bits; skip_inside: the skip rule also
@@ -218,13 +233,15 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                                                     bool skip_inside)
 {
     const int32_t H = static_cast<int32_t>(p.H), W = static_cast<int32_t>(p.W);
-    const float Hf = static_cast<float>(p.H), Wf = static_cast<float>(p.W);
+    const float Hf = p.Hf, Wf = p.Wf;
     const float* m = p.tf + 16 * b;
     // rows x, y and the divisor row (w for OpenGL, z for OpenCV)
     const float4 rx = *reinterpret_cast<const float4*>(m);
     const float4 ry = *reinterpret_cast<const float4*>(m + 4);
     const float4 rd = *reinterpret_cast<const float4*>(m + (OPENGL ? 12 : 8));
     const float* sat_b = p.sat + b * p.H * p.W;
+    const float in_hx = __fsub_rn(Wf, 1.5f), in_hy = __fsub_rn(Hf, 1.5f);
+    const float in2_hx = __fsub_rn(Wf, 2.5f), in2_hy = __fsub_rn(Hf, 2.5f);
     ItemResult out{ 0, 0, 0, 0 };
     Box prev[4];
     uint32_t prev_in = 0, prev_in2 = 0, prev_front = 0;
@@ -266,11 +283,11 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                     front9 |= 1u << k;
                 if (PARTIAL)
                 {
-                    const int32_t qx = f2i32(roundf(px[k]));
-                    const int32_t qy = f2i32(roundf(py[k]));
-                    if (1 <= qy && qy < H - 1 && 1 <= qx && qx < W - 1)
+                    // 1 <= round(q) < size - 1 (round half away from zero)
+                    // exactly when 0.5 <= q < size - 1.5; NaN fails both
+                    if (px[k] >= 0.5f && px[k] < in_hx && py[k] >= 0.5f && py[k] < in_hy)
                         in9 |= 1u << k;
-                    if (skip_inside && 2 <= qy && qy < H - 2 && 2 <= qx && qx < W - 2)
+                    if (skip_inside && px[k] >= 1.5f && px[k] < in2_hx && py[k] >= 1.5f && py[k] < in2_hy)
                         in9b |= 1u << k;
                 }
             }
@@ -303,7 +320,7 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                 const uint32_t bit = 1u << (c + 4 * (z - 1));
                 const bool front = (prev_front & cur_front & cbit) != 0;
                 const bool in2 = (prev_in2 & cur_in2 & cbit) != 0;
-                const ViewResult r = classify_view<PARTIAL>(sat_b, H, W, merge(prev[c], cur[c]),
+                const ViewResult r = classify_view<PARTIAL>(sat_b, H, W, Hf, Wf, merge(prev[c], cur[c]),
                                                             want_skip && front && (!skip_inside || in2));
                 if (r.cls == kEmpty)
                     out.empty |= bit;

@@ -140,6 +140,53 @@ __device__ __forceinline__ int64_t f2i64(float f)
     return __float2ll_rz(f);
 }
 
+// Exact conversions between small non-negative integers and floats with
+// adds and bit moves only: the conversion instructions run on narrow pipes
+// (the 64-bit ones on the FP64 pipe) and bound the carve otherwise.  Floats
+// in [2^23, 2^24) are spaced 1 apart, so 2^23 + n carries the integer n in
+// its low mantissa bits.
+constexpr float kTwo23 = 8388608.f;
+constexpr int32_t kTwo23Bits = 0x4B000000;
+
+// float(n) for n in [0, 2^23).
+__device__ __forceinline__ float small_i2f(int32_t n)
+{
+    return __fsub_rn(__int_as_float(kTwo23Bits | n), kTwo23);
+}
+
+struct Snapped
+{
+    int32_t i; // the integer
+    float f;   // the same integer as a float
+};
+
+// roundf(v) (half away from zero) clamped to [0, hi], hi an integer below
+// 2^23.  Rounding commutes with clamping to integer bounds; for y >= 0,
+// round(y) = floor(y + 0.5), and y + 0.5 rounded toward zero keeps that floor
+// because every integer below 2^24 is a float; the second add toward zero then
+// leaves 2^23 + floor.  NaN clamps to 0, as a saturating conversion and the
+// clamp do.
+__device__ __forceinline__ Snapped round_clamp(float v, float hi)
+{
+    const float y = fminf(fmaxf(v, 0.f), hi);
+    const float t = __fadd_rz(__fadd_rz(y, 0.5f), kTwo23);
+    return Snapped{ __float_as_int(t) - kTwo23Bits, __fsub_rn(t, kTwo23) };
+}
+
+// roundf(v) for |v| < 2^22 (round_clamp's adds on |v|, then the sign); false
+// (and nothing written) otherwise, NaN included.
+__device__ __forceinline__ bool round_small(float v, Snapped& out)
+{
+    const float a = fabsf(v);
+    if (!(a < 4194304.f))
+        return false;
+    const float t = __fadd_rz(__fadd_rz(a, 0.5f), kTwo23);
+    const int32_t n = __float_as_int(t) - kTwo23Bits;
+    const float nf = __fsub_rn(t, kTwo23);
+    out = Snapped{ v < 0.f ? -n : n, copysignf(nf, v) }; // roundf(-0.f) is -0.f
+    return true;
+}
+
 // K*T*[x,y,z,1] with nested fmaf (visual_hull_cuda.cu:142-156). m is row-major 4x4.
 __device__ __forceinline__ float project_row(const float* m, float x, float y, float z)
 {
@@ -156,8 +203,9 @@ __device__ __forceinline__ void to_pixel(const float* m, float x, float y, float
         float cw = project_row(m + 12, x, y, z);
         float nx = __fdiv_rn(cx, cw);
         float ny = __fdiv_rn(cy, cw);
-        px = __fsub_rn(__fdiv_rn(__fmul_rn(__fadd_rn(nx, 1.f), W), 2.f), 0.5f);
-        py = __fsub_rn(__fdiv_rn(__fmul_rn(__fadd_rn(ny, 1.f), H), 2.f), 0.5f);
+        // x / 2 == x * 0.5 exactly
+        px = __fsub_rn(__fmul_rn(__fmul_rn(__fadd_rn(nx, 1.f), W), 0.5f), 0.5f);
+        py = __fsub_rn(__fmul_rn(__fmul_rn(__fadd_rn(ny, 1.f), H), 0.5f), 0.5f);
     }
     else
     {
