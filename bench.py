@@ -23,6 +23,8 @@ requests (weak scaling, no collective on the data path).
 
 --mode hetero: 64 heterogeneous requests (views U{4..48}, side
 U{256,512,768,1024}, level U{6..9}, partial ~ Bernoulli(0.3)), batched vs plain.
+--mode mc: torchhull.marching_cubes on the reference benchmark's sphere SDF
+volumes (100^3 .. 600^3, dense and sparse), ms per call.
 --mode serve: Poisson arrivals (default 200/s for 10 s) from a pool of
 pregenerated requests of the heterogeneous distribution plus 2 % large ones
 (64 views of 2048^2, level 10) through the continuous-batching server (60 GB
@@ -234,6 +236,8 @@ def run_gb300(args) -> dict | None:
         return finish(run_hetero(args, th, scenes, dev, world, rank), world)
     if args.mode == "serve":
         return finish(run_serve(args, th, scenes, dev, world, rank), world)
+    if args.mode == "mc":
+        return finish(run_mc(args, th, dev, world, rank), world)
 
     Q = args.requests
     reqs = [scenes.partial_request(device=dev, seed=3 + 1000 * rank + q) for q in range(Q)]
@@ -389,6 +393,60 @@ def run_hetero(args, th, scenes, dev, world, rank):
     }
 
 
+def sphere_sdf(size: int, dev):
+    """The reference benchmark's volume (benchmarks/test_bench_marching_cubes.py:68-86)."""
+    import torch
+
+    g = torch.arange(size, device=dev)
+    pts = torch.stack(torch.meshgrid(3 * [g], indexing="ij"), dim=0).reshape(3, -1).T.to(torch.float32)
+    center = torch.full((3,), size / 2, dtype=torch.float32, device=dev)
+    radius = 0.8731945 * (size / 2)
+    return (torch.linalg.norm(pts - center[None], dim=1) - radius).reshape(1, size, size, size)
+
+
+def run_mc(args, th, dev, world, rank):
+    """Marching cubes on the reference benchmark's sphere volumes, dense and sparse (truncation 2)."""
+    import torch
+
+    rows = []
+    for size in (100, 200, 300, 400, 500, 600):
+        dense = sphere_sdf(size, dev)
+        sparse_src = dense.clone()
+        sparse_src[sparse_src.abs() > 2] = 0
+        sparse = sparse_src.to_sparse()
+        del sparse_src
+        for kind, vol in (("dense", dense), ("sparse", sparse)):
+            for _ in range(max(3, args.warmup)):
+                v, f = th.marching_cubes(vol, 0.0, False)
+            torch.cuda.synchronize()
+            times = []
+            for _ in range(args.steps):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                th.marching_cubes(vol, 0.0, False)
+                e1.record()
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+            times.sort()
+            nbytes = dense.numel() * 4 if kind == "dense" else vol.values().numel() * (4 + 32)
+            rows.append({"size": size, "kind": kind, "p50_ms": percentile(times, 50), "min_ms": times[0],
+                         "verts": int(v.shape[0]), "faces": int(f.shape[0]), "input_bytes": nbytes,
+                         "input_gbs": nbytes / (percentile(times, 50) / 1000.0) / 1e9})
+        del dense, sparse
+        torch.cuda.empty_cache()
+    if rank != 0:
+        return None
+    head = next(r for r in rows if r["size"] == 600 and r["kind"] == "dense")
+    return {"metric": "marching_cubes ms per call, 600^3 dense float32 sphere SDF (reference benchmark volumes)",
+            "value": head["p50_ms"], "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": head["p50_ms"], "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic: sphere SDF of benchmarks/test_bench_marching_cubes.py",
+            "config": {"workload": "torchhull.marching_cubes(sdf, isolevel=0, return_local_coords=False), sizes "
+                                   "100..600, dense and sparse (|sdf| <= 2)"},
+            "table": rows}
+
+
 def run_serve(args, th, scenes, dev, world, rank):
     import numpy as np
     import torch
@@ -512,7 +570,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--mode", choices=["headline", "hetero", "serve"], default="headline")
+    ap.add_argument("--mode", choices=["headline", "hetero", "serve", "mc"], default="headline")
     ap.add_argument("--requests", type=int, default=4)
     ap.add_argument("--cpu-samples", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")

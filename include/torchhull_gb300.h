@@ -177,6 +177,41 @@ th_status th_integral_image(th_context* ctx,
                             void* stream);
 
 /*
+ * Marching cubes over a dense volume or a coalesced sparse COO volume.
+ * Replaces torchhull::marching_cubes (src/torchhull/_C/include/torchhull/
+ * marching_cubes.h:11-15; marching_cubes_cuda.cu:376-533 dense, :754-831
+ * sparse).  Two calls, as for th_visual_hull: th_marching_cubes computes the
+ * mesh sizes (one device->host read), th_marching_cubes_export writes the
+ * mesh into caller buffers (verts [num_verts,3] float32, faces [num_faces,3]
+ * int64).  Axes: x along the volume's last dimension (width), z along its
+ * first (depth).
+ */
+typedef struct th_mc_args
+{
+    int32_t sparse;         /* 0: dense volume, 1: sparse COO volume */
+    int32_t dtype;          /* float16, float32, float64: the volume's or the values' type */
+    int64_t depth;          /* sizes of the [1, D, H, W] volume */
+    int64_t height;
+    int64_t width;
+    const void* volume;     /* dense: D*H*W contiguous elements, width fastest */
+    const int64_t* indices; /* sparse: [4, nnz] row-major, rows (0, z, y, x), strictly ascending in (z, y, x) */
+    const void* values;     /* sparse: [nnz] contiguous */
+    int64_t nnz;
+    float isolevel;         /* >= 0 */
+    int32_t return_local_coords; /* 1: [-1, 1]^3, 0: voxel coordinates */
+    int32_t unique_verts;        /* 1: shared vertices, 0: triangle soup */
+} th_mc_args;
+
+typedef struct th_mc_info
+{
+    int64_t num_verts;
+    int64_t num_faces;
+} th_mc_info;
+
+th_status th_marching_cubes(th_context* ctx, const th_mc_args* args, void* stream, th_mc_info* info);
+th_status th_marching_cubes_export(th_context* ctx, float* verts, int64_t* faces, void* stream);
+
+/*
  * Batched form: n independent requests processed together (shared launches,
  * one device->host read for all).  infos[n] receives the sizes; results stay
  * in the context until the next batched call.  No counterpart in the

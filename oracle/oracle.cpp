@@ -1047,3 +1047,232 @@ extern "C" int oracle_gaussian_blur(const void* images,
     });
     return 0;
 }
+
+// ---------------------------------------------------------------------------
+// public marching cubes (marching_cubes_cuda.cu:146-374 kernels, :376-533
+// dense driver, :535-831 sparse driver), over a list of grid points
+
+namespace
+{
+
+struct McGrid
+{
+    int64_t W, H, D; // sizes along x, y, z
+};
+
+int64_t mc_ravel(const I3& p, const McGrid& g)
+{
+    return p.x + g.W * (p.y + g.H * p.z);
+}
+
+I3 mc_unravel(int64_t id, const McGrid& g)
+{
+    I3 p;
+    p.x = id % g.W;
+    p.y = (id / g.W) % g.H;
+    p.z = id / (g.W * g.H);
+    return p;
+}
+
+// points: strictly ascending ravel ids; values: each point's value as a double
+// (exact for half, float and double volumes).  A dense volume is the list of
+// all its points, which turns the dense driver's cell loop (:146-178) into the
+// sparse driver's entry loop (:180-223) over the same cells in the same order.
+Mesh marching_cubes_points(const std::vector<int64_t>& ids,
+                           const std::vector<double>& vals,
+                           const McGrid& grid,
+                           float iso,
+                           bool unique_verts,
+                           bool local,
+                           int nthreads)
+{
+    Mesh mesh;
+    const int64_t N = static_cast<int64_t>(ids.size());
+    if (N == 0)
+        return mesh;
+    auto find = [&](int64_t key) -> int64_t {
+        auto it = std::lower_bound(ids.begin(), ids.end(), key);
+        return (it != ids.end() && *it == key) ? (it - ids.begin()) : -1;
+    };
+    // value < isolevel in the value's type (:166-171); val[] holds floats (:338-343)
+    auto below = [&](int64_t k) { return vals[k] < static_cast<double>(iso); };
+
+    std::vector<uint8_t> code(N, 0);
+    std::vector<int64_t> count(N, 0);
+    parallel_for(N, nthreads, [&](int64_t t0, int64_t t1) {
+        for (int64_t t = t0; t < t1; ++t)
+        {
+            I3 g = mc_unravel(ids[t], grid);
+            uint8_t c = 0;
+            if (g.x < grid.W - 1 && g.y < grid.H - 1 && g.z < grid.D - 1)
+            {
+                for (int i = 0; i < 8; ++i)
+                {
+                    int64_t k = find(mc_ravel(cube_vertex(g, i), grid));
+                    if (k < 0)
+                    {
+                        c = 0;
+                        break;
+                    }
+                    if (below(k))
+                        c |= static_cast<uint8_t>(1u << i);
+                }
+            }
+            code[t] = c;
+            count[t] = MC_COUNT[c];
+        }
+    });
+
+    std::vector<int64_t> offset(N + 1, 0);
+    for (int64_t t = 0; t < N; ++t)
+        offset[t + 1] = offset[t] + count[t];
+    const int64_t V = offset[N];
+    if (V == 0)
+        return mesh;
+
+    // generate_faces_{dense,sparse} (:242-374)
+    std::vector<float> soup(3 * V);
+    std::vector<int64_t> edge_ids(unique_verts ? V : 0);
+    parallel_for(N, nthreads, [&](int64_t t0, int64_t t1) {
+        for (int64_t t = t0; t < t1; ++t)
+        {
+            uint8_t c = code[t];
+            if (MC_COUNT[c] == 0)
+                continue;
+            I3 g = mc_unravel(ids[t], grid);
+            for (int j = 0; j < MC_COUNT[c]; ++j)
+            {
+                uint8_t e = MC_EDGES[c][j];
+                int lo = e & 7, axis = e >> 3;
+                I3 p1 = cube_vertex(g, lo);
+                I3 p2 = cube_vertex(g, lo | (1 << axis));
+                float v1 = static_cast<float>(vals[find(mc_ravel(p1, grid))]);
+                float v2 = static_cast<float>(vals[find(mc_ravel(p2, grid))]);
+                F3 v = interpolate_vertex(iso, p1, p2, v1, v2);
+                int64_t o = offset[t] + j;
+                soup[3 * o + 0] = v.x;
+                soup[3 * o + 1] = v.y;
+                soup[3 * o + 2] = v.z;
+                if (unique_verts)
+                    edge_ids[o] = (mc_ravel(p1, grid) << 3) | (int64_t{ 1 } << axis); // hash_edge (:99-112)
+            }
+        }
+    });
+
+    // unique_dim(sorted, return_inverse) + index_put_ (:500-511)
+    if (unique_verts)
+    {
+        std::vector<int64_t> order(V);
+        std::iota(order.begin(), order.end(), 0);
+        std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return edge_ids[a] < edge_ids[b]; });
+        std::vector<int64_t> inverse(V);
+        int64_t u = -1;
+        int64_t prev = -1;
+        for (int64_t k = 0; k < V; ++k)
+        {
+            int64_t o = order[k];
+            if (k == 0 || edge_ids[o] != prev)
+            {
+                ++u;
+                prev = edge_ids[o];
+                mesh.verts.push_back(soup[3 * o + 0]);
+                mesh.verts.push_back(soup[3 * o + 1]);
+                mesh.verts.push_back(soup[3 * o + 2]);
+            }
+            inverse[o] = u;
+        }
+        mesh.faces = std::move(inverse);
+    }
+    else
+    {
+        mesh.verts = std::move(soup);
+        mesh.faces.resize(V);
+        std::iota(mesh.faces.begin(), mesh.faces.end(), 0);
+    }
+
+    // local coordinates: verts * (2 / (size - 1)) - 1, two rounded operations (:513-520)
+    if (local)
+    {
+        const float scale[3] = { 2.f / static_cast<float>(grid.W - 1), 2.f / static_cast<float>(grid.H - 1),
+                                 2.f / static_cast<float>(grid.D - 1) };
+        for (size_t i = 0; i < mesh.verts.size(); i += 3)
+            for (int a = 0; a < 3; ++a)
+            {
+                const float m = mesh.verts[i + a] * scale[a];
+                mesh.verts[i + a] = m - 1.f;
+            }
+    }
+    return mesh;
+}
+
+} // namespace
+
+struct oracle_mesh
+{
+    Mesh mesh;
+};
+
+extern "C" {
+
+oracle_mesh* oracle_marching_cubes(const int64_t* ids,
+                                   const void* values,
+                                   int values_dtype,
+                                   int64_t n,
+                                   int64_t depth,
+                                   int64_t height,
+                                   int64_t width,
+                                   float isolevel,
+                                   int return_local_coords,
+                                   int unique_verts,
+                                   int nthreads,
+                                   char* err,
+                                   int errlen)
+{
+    if (!(values_dtype == ORACLE_FLOAT16 || values_dtype == ORACLE_FLOAT32 || values_dtype == ORACLE_FLOAT64))
+    {
+        set_err(err, errlen, std::string("marching cubes not implemented for '") + dtype_name(values_dtype) + "'");
+        return nullptr;
+    }
+    if (depth < 2 || height < 2 || width < 2)
+    {
+        set_err(err, errlen, "volume sizes must be at least 2");
+        return nullptr;
+    }
+    std::vector<int64_t> pts(ids, ids + n);
+    for (int64_t i = 1; i < n; ++i)
+        if (pts[i] <= pts[i - 1])
+        {
+            set_err(err, errlen, "point ids must be strictly ascending");
+            return nullptr;
+        }
+    std::vector<double> vals(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i)
+        vals[i] = load_as_double(values, values_dtype, i);
+    auto* out = new oracle_mesh;
+    out->mesh = marching_cubes_points(pts, vals, McGrid{ width, height, depth }, isolevel, unique_verts != 0,
+                                      return_local_coords != 0, nthreads);
+    return out;
+}
+
+int64_t oracle_mesh_num_verts(const oracle_mesh* m)
+{
+    return static_cast<int64_t>(m->mesh.verts.size() / 3);
+}
+
+int64_t oracle_mesh_num_faces(const oracle_mesh* m)
+{
+    return static_cast<int64_t>(m->mesh.faces.size() / 3);
+}
+
+void oracle_mesh_copy(const oracle_mesh* m, float* verts, int64_t* faces)
+{
+    std::copy(m->mesh.verts.begin(), m->mesh.verts.end(), verts);
+    std::copy(m->mesh.faces.begin(), m->mesh.faces.end(), faces);
+}
+
+void oracle_mesh_free(oracle_mesh* m)
+{
+    delete m;
+}
+
+} // extern "C"

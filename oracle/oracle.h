@@ -92,6 +92,32 @@ int oracle_gaussian_blur(const void* images,
                          char* err,
                          int errlen);
 
+typedef struct oracle_mesh oracle_mesh;
+
+// marching_cubes (marching_cubes_cuda.cu:146-374 kernels, :376-831 drivers)
+// over a list of grid points of a [1, depth, height, width] volume: ids are
+// ravel indices x + width (y + height z), strictly ascending (all points for
+// a dense volume, the coalesced entries for a sparse one); values: [n] of
+// values_dtype (float16, float32, float64).  Returns NULL and fills err on an
+// argument error.
+oracle_mesh* oracle_marching_cubes(const int64_t* ids,
+                                   const void* values,
+                                   int values_dtype,
+                                   int64_t n,
+                                   int64_t depth,
+                                   int64_t height,
+                                   int64_t width,
+                                   float isolevel,
+                                   int return_local_coords,
+                                   int unique_verts,
+                                   int nthreads,
+                                   char* err,
+                                   int errlen);
+int64_t oracle_mesh_num_verts(const oracle_mesh* m);
+int64_t oracle_mesh_num_faces(const oracle_mesh* m);
+void oracle_mesh_copy(const oracle_mesh* m, float* verts, int64_t* faces);
+void oracle_mesh_free(oracle_mesh* m);
+
 #ifdef __cplusplus
 }
 #endif

@@ -63,6 +63,13 @@ def lib() -> ctypes.CDLL:
         L.oracle_integral_image.argtypes = [vp, i32, i64, i64, i64, vp, i32]
         L.oracle_gaussian_blur.restype = i32
         L.oracle_gaussian_blur.argtypes = [vp, i32, i64, i64, i64, i32, f32, i32, vp, i32, i32, ctypes.c_char_p, i32]
+        L.oracle_marching_cubes.restype = vp
+        L.oracle_marching_cubes.argtypes = [vp, vp, i32, i64, i64, i64, i64, f32, i32, i32, i32, ctypes.c_char_p, i32]
+        for name in ("oracle_mesh_num_verts", "oracle_mesh_num_faces"):
+            getattr(L, name).restype = i64
+            getattr(L, name).argtypes = [vp]
+        L.oracle_mesh_copy.argtypes = [vp, vp, vp]
+        L.oracle_mesh_free.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -138,6 +145,36 @@ def gaussian_blur(images, kernel_size, sigma, sparse=True, dtype=None, nthreads=
     if rc != 0:
         raise RuntimeError(err.value.decode())
     return out
+
+
+def marching_cubes(volume=None, isolevel=0.0, return_local_coords=True, unique_verts=True, *, indices=None,
+                   values=None, size=None, nthreads=0) -> tuple[np.ndarray, np.ndarray]:
+    """Dense volume [1,D,H,W], or a coalesced sparse one as indices [4,N] (rows 0, z, y, x), values [N] and
+    size (1, D, H, W).  Returns (verts [V,3] float32, faces [F,3] int64)."""
+    if volume is not None:
+        v = _as_array(volume)
+        _, D, H, W = v.shape
+        vals = np.ascontiguousarray(v.reshape(-1))
+        ids = np.arange(vals.size, dtype=np.int64)
+    else:
+        idx = _as_array(indices).astype(np.int64)
+        vals = _as_array(values)
+        _, D, H, W = size
+        ids = np.ascontiguousarray(idx[3] + W * (idx[2] + H * idx[1]), dtype=np.int64)
+    err = ctypes.create_string_buffer(256)
+    L = lib()
+    h = L.oracle_marching_cubes(ids.ctypes.data, vals.ctypes.data, DTYPE_CODES.get(vals.dtype, -1), ids.size, D, H,
+                                W, float(isolevel), int(bool(return_local_coords)), int(bool(unique_verts)),
+                                int(nthreads), err, len(err))
+    if not h:
+        raise RuntimeError(err.value.decode())
+    try:
+        verts = np.empty((L.oracle_mesh_num_verts(h), 3), dtype=np.float32)
+        faces = np.empty((L.oracle_mesh_num_faces(h), 3), dtype=np.int64)
+        L.oracle_mesh_copy(h, verts.ctypes.data, faces.ctypes.data)
+    finally:
+        L.oracle_mesh_free(h)
+    return verts, faces
 
 
 def nthreads_default() -> int:

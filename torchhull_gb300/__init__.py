@@ -1,7 +1,8 @@
 """GB300 (sm_103a) implementation of torchhull's visual-hull and blur path.
 
 Drop-in for ``torchhull.visual_hull``, ``torchhull.visual_hull_with_candidate_voxels``,
-``torchhull.sparse_visual_hull_field`` and ``torchhull.gaussian_blur``: same
+``torchhull.sparse_visual_hull_field``, ``torchhull.marching_cubes`` and
+``torchhull.gaussian_blur``: same
 argument names, defaults, outputs and errors.  The work runs in hand-written
 CUDA behind the C ABI of ``include/torchhull_gb300.h``; there is no CPU path,
 and CPU tensors raise the reference's "No backend implementation" error.
@@ -23,6 +24,7 @@ from . import build as _build
 __all__ = [
     "gaussian_blur",
     "integral_image",
+    "marching_cubes",
     "sparse_visual_hull_field",
     "visual_hull",
     "visual_hull_with_candidate_voxels",
@@ -49,6 +51,7 @@ visual_hull = _C.visual_hull
 visual_hull_with_candidate_voxels = _C.visual_hull_with_candidate_voxels
 gaussian_blur = _C.gaussian_blur
 integral_image = _C.integral_image
+marching_cubes = _C.marching_cubes
 
 
 def sparse_visual_hull_field(

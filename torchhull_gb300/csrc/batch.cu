@@ -47,6 +47,9 @@ __global__ void batch_init_kernel(BatchPlan bp)
         bp.ctr->count[0] = bp.nreq;
 }
 
+// VARIANT: (partial << 1) | opengl shared by every request of the batch, or
+// -1 to branch per request.
+template <int VARIANT>
 __device__ __forceinline__ ItemResult batch_item(const BatchReq& q,
                                                  int64_t b,
                                                  const float wx[3],
@@ -56,6 +59,8 @@ __device__ __forceinline__ ItemResult batch_item(const BatchReq& q,
                                                  bool skip_inside)
 {
     const ViewSource src = make_view_source(q.tf, q.sat, q.H, q.W);
+    if constexpr (VARIANT >= 0)
+        return classify_item<(VARIANT >> 1) != 0, (VARIANT & 1) != 0>(src, b, wx, wy, wz, want_skip, skip_inside);
     if (q.partial)
         return q.opengl ? classify_item<true, true>(src, b, wx, wy, wz, want_skip, skip_inside)
                         : classify_item<true, false>(src, b, wx, wy, wz, want_skip, skip_inside);
@@ -71,6 +76,7 @@ __device__ __forceinline__ int64_t level_entries(const BatchPlan& bp, int li, in
     return n < room ? n : (room > 0 ? room : 0);
 }
 
+template <int VARIANT>
 __global__ void __launch_bounds__(32 * kBatchWarps) batch_carve_kernel(BatchPlan bp)
 {
     cg::grid_group grid = cg::this_grid();
@@ -138,7 +144,7 @@ __global__ void __launch_bounds__(32 * kBatchWarps) batch_carve_kernel(BatchPlan
                     lattice_world(qq.corner, qq.length, is & kCellMask, li, inv_rc, wx, wy, wz);
                     produce = qq.skip_ok && (*qq.nonbinary == 0) && (li + 1 < qq.level);
                     const bool skip_inside = qq.partial && (li + 1 == qq.level - 1);
-                    res = batch_item(qq, b, wx, wy, wz, produce && b < 32, skip_inside);
+                    res = batch_item<VARIANT>(qq, b, wx, wy, wz, produce && b < 32, skip_inside);
                 }
                 const int seg = act ? s : -1 - lane;
                 const int prev_seg = __shfl_up_sync(0xffffffffu, seg, 1);
@@ -254,13 +260,31 @@ void launch_batch_carve(const BatchPlan& bp, cudaStream_t s)
 {
     if (bp.max_level <= 0)
         return;
+    void (*kernel)(BatchPlan) = batch_carve_kernel<-1>;
+    switch (bp.variant)
+    {
+    case 0:
+        kernel = batch_carve_kernel<0>;
+        break;
+    case 1:
+        kernel = batch_carve_kernel<1>;
+        break;
+    case 2:
+        kernel = batch_carve_kernel<2>;
+        break;
+    case 3:
+        kernel = batch_carve_kernel<3>;
+        break;
+    default:
+        break;
+    }
     int per_sm = 0;
-    TH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_carve_kernel, 32 * kBatchWarps, 0));
+    TH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * kBatchWarps, 0));
     if (per_sm < 1)
         throw CudaError{ cudaErrorLaunchOutOfResources, "batch carve kernel does not fit on an SM" };
     BatchPlan arg = bp;
     void* args[] = { &arg };
-    TH_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(batch_carve_kernel), dim3(per_sm * sm_count()),
+    TH_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(kernel), dim3(per_sm * sm_count()),
                                         dim3(32 * kBatchWarps), args, 0, s));
     note_launches(1);
 }

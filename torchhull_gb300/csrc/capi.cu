@@ -17,9 +17,12 @@
 #include <string>
 #include <vector>
 
+#include <sstream>
+
 #include "th_batch.cuh"
 #include "th_hull.cuh"
 #include "th_internal.h"
+#include "th_mc.cuh"
 
 namespace th
 {
@@ -264,6 +267,38 @@ struct BatchState
 } // namespace
 } // namespace th
 
+namespace th
+{
+namespace
+{
+
+// Pools and the last result of the public marching cubes.
+struct McSlot
+{
+    DevBuf groups, keys, slots, codes, used, vbase, tiles_soup, tiles_verts, ctr;
+    McCounters* host = nullptr; // pinned copy of the counters
+    McPlan plan{};
+    th_mc_info info{};
+    bool has_result = false;
+
+    std::vector<const DevBuf*> buffers() const
+    {
+        return { &groups, &keys, &slots, &codes, &used, &vbase, &tiles_soup, &tiles_verts, &ctr };
+    }
+
+    void release()
+    {
+        for (const DevBuf* b : buffers())
+            const_cast<DevBuf*>(b)->release();
+        if (host)
+            cudaFreeHost(host);
+        host = nullptr;
+    }
+};
+
+} // namespace
+} // namespace th
+
 struct th_context
 {
     int device = 0;
@@ -272,6 +307,7 @@ struct th_context
     std::vector<th::HullSlot> batch;
     th::BatchState bstate;
     th::DevBuf blur_scratch;
+    th::McSlot mc;
     bool profiling = false;
     th::StageEvents events;
     th_stage_times times{};
@@ -294,6 +330,8 @@ int64_t pool_bytes(const th_context* ctx)
         return b;
     };
     int64_t total = sum(ctx->hull) + static_cast<int64_t>(ctx->blur_scratch.bytes);
+    for (const DevBuf* d : ctx->mc.buffers())
+        total += static_cast<int64_t>(d->bytes);
     for (const auto& s : ctx->batch)
         total += sum(s);
     return total;
@@ -711,6 +749,15 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
         bp.node_skip = bs.node_skip.as<uint32_t>();
         bp.node_cap = bs.node_cap;
         bp.ctr = bs.ctr.as<BatchCounters>();
+        bp.variant = -1;
+        for (int32_t r = 0; r < n; ++r)
+        {
+            const BatchReq& q = bs.host_reqs[r];
+            const int32_t v = (q.partial << 1) | q.opengl;
+            bp.variant = (r == 0 || bp.variant == v) ? v : -2;
+        }
+        if (bp.variant < 0)
+            bp.variant = -1;
         launch_batch_init(bp, st);
         launch_batch_carve(bp, st);
         launch_batch_mark(bp, st);
@@ -817,6 +864,135 @@ th_status guarded(th_context* ctx, F&& f)
 } // namespace
 } // namespace th
 
+namespace th
+{
+namespace
+{
+
+std::string float_text(float v)
+{
+    std::ostringstream os;
+    os << v;
+    return os.str();
+}
+
+// Argument checks of marching_cubes_cuda_{dense,sparse} (:382-385, :758-764,
+// :789-795) that reach the C ABI; the tensor-layout checks live in the torch layer.
+void run_mc(McSlot& s, const th_mc_args* a, cudaStream_t st)
+{
+    s.has_result = false;
+    if (!a)
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "args is NULL" };
+    if (a->depth < 0 || a->height < 0 || a->width < 0 || a->nnz < 0)
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "volume sizes must be non-negative" };
+    if (!(a->isolevel >= 0.f))
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: isolevel >= 0 (" + float_text(a->isolevel) + " vs. 0)" };
+    const char* kernel = a->sparse ? "classify_voxels_sparse" : "classify_voxels_dense";
+    if (!(a->dtype == TH_FLOAT16 || a->dtype == TH_FLOAT32 || a->dtype == TH_FLOAT64))
+        throw ArgError{ TH_ERR_UNSUPPORTED_DTYPE,
+                        std::string("\"") + kernel + "\" not implemented for '" + dtype_name(a->dtype) + "'" };
+    const int64_t D = a->depth, H = a->height, W = a->width;
+    McPlan p{};
+    p.dtype = a->dtype;
+    p.sparse = a->sparse != 0;
+    p.unique = a->unique_verts != 0;
+    p.local = a->return_local_coords != 0;
+    p.D = D;
+    p.H = H;
+    p.W = W;
+    p.iso = a->isolevel;
+    // 2.f / static_cast<float>(size - 1) (:515-517), x along W
+    p.scale[0] = 2.f / static_cast<float>(W - 1);
+    p.scale[1] = 2.f / static_cast<float>(H - 1);
+    p.scale[2] = 2.f / static_cast<float>(D - 1);
+    if (p.sparse)
+    {
+        if (a->nnz >= (int64_t{ 1 } << 31))
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "sparse volumes hold fewer than 2^31 values" };
+        if (a->nnz > 0 && (!a->indices || !a->values))
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "indices or values pointer is NULL" };
+        p.indices = a->indices;
+        p.values = a->values;
+        p.nnz = a->nnz;
+    }
+    else
+    {
+        // the dense driver sizes its cell arrays (D-1)(H-1)(W-1) and reads the
+        // last scan entry back (:392-397, :421-423)
+        const int64_t cells = (D - 1) * (H - 1) * (W - 1);
+        if (D < 1 || H < 1 || W < 1)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Trying to create tensor with negative dimension " +
+                                                             std::to_string(cells) + ": [" + std::to_string(cells) + "]" };
+        if (cells == 0)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "index -1 is out of bounds for dimension 0 with size 0" };
+        if (!a->volume)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "volume pointer is NULL" };
+        p.volume = a->volume;
+        p.points = D * H * W;
+        p.wide = p.points >= (int64_t{ 1 } << 32);
+        p.ngroups = (p.points + 31) / 32;
+    }
+
+    if (!s.host)
+        TH_CUDA(cudaMallocHost(&s.host, sizeof(McCounters)));
+    s.ctr.ensure(sizeof(McCounters));
+    p.ctr = s.ctr.as<McCounters>();
+    if (p.sparse)
+    {
+        const int64_t n = p.nnz;
+        uint64_t cap = 64;
+        while (cap < 2 * static_cast<uint64_t>(n))
+            cap <<= 1;
+        s.keys.ensure(sizeof(unsigned long long) * cap);
+        s.slots.ensure(sizeof(int32_t) * cap);
+        s.codes.ensure(static_cast<size_t>(n));
+        s.tiles_soup.ensure(sizeof(unsigned long long) * mc_scan_tiles(n));
+        p.keys = s.keys.as<unsigned long long>();
+        p.slots = s.slots.as<int32_t>();
+        p.hmask = cap - 1;
+        p.codes = s.codes.as<uint8_t>();
+        p.tiles_soup = s.tiles_soup.as<unsigned long long>();
+        if (p.unique)
+        {
+            s.used.ensure(sizeof(uint32_t) * n);
+            s.vbase.ensure(sizeof(unsigned long long) * n);
+            s.tiles_verts.ensure(sizeof(unsigned long long) * mc_scan_tiles(n));
+            p.used = s.used.as<uint32_t>();
+            p.vbase = s.vbase.as<unsigned long long>();
+            p.tiles_verts = s.tiles_verts.as<unsigned long long>();
+        }
+    }
+    else
+    {
+        s.tiles_soup.ensure(sizeof(unsigned long long) * mc_scan_tiles(p.points));
+        p.tiles_soup = s.tiles_soup.as<unsigned long long>();
+        if (p.unique)
+        {
+            s.groups.ensure(sizeof(McGroup) * p.ngroups);
+            s.tiles_verts.ensure(sizeof(unsigned long long) * mc_scan_tiles(p.ngroups));
+            p.groups = s.groups.as<McGroup>();
+            p.tiles_verts = s.tiles_verts.as<unsigned long long>();
+        }
+    }
+
+    launch_mc_count(p, st);
+    TH_CUDA(cudaMemcpyAsync(s.host, p.ctr, sizeof(McCounters), cudaMemcpyDeviceToHost, st));
+    TH_CUDA(cudaStreamSynchronize(st));
+    const McCounters& c = *s.host;
+    if (c.flags & kMcBadIndex)
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "sparse volume indices lie outside the volume" };
+    if (c.flags & kMcUnsorted)
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT,
+                        "sparse volume indices must be coalesced (strictly ascending in (z, y, x))" };
+    s.plan = p;
+    s.info.num_faces = static_cast<int64_t>(c.soup / 3);
+    s.info.num_verts = static_cast<int64_t>(p.unique ? c.verts : c.soup);
+    s.has_result = true;
+}
+
+} // namespace
+} // namespace th
+
 using namespace th;
 
 extern "C" {
@@ -849,6 +1025,7 @@ void th_context_destroy(th_context* ctx)
     for (auto& s : ctx->batch)
         s.release();
     ctx->blur_scratch.release();
+    ctx->mc.release();
     ctx->bstate.release();
     ctx->events.destroy();
     for (auto& e : ctx->tune_ev)
@@ -1052,6 +1229,30 @@ th_status th_integral_image(th_context* ctx,
         if (!masks || !out)
             throw ArgError{ TH_ERR_INVALID_ARGUMENT, "masks or out pointer is NULL" };
         launch_integral_image(masks, masks_dtype, batch, height, width, out, static_cast<cudaStream_t>(stream));
+    });
+}
+
+th_status th_marching_cubes(th_context* ctx, const th_mc_args* args, void* stream, th_mc_info* info)
+{
+    return guarded(ctx, [&] {
+        run_mc(ctx->mc, args, static_cast<cudaStream_t>(stream));
+        if (info)
+            *info = ctx->mc.info;
+    });
+}
+
+th_status th_marching_cubes_export(th_context* ctx, float* verts, int64_t* faces, void* stream)
+{
+    return guarded(ctx, [&] {
+        McSlot& s = ctx->mc;
+        if (!s.has_result)
+            throw ArgError{ TH_ERR_STATE, "th_marching_cubes_export called without a successful th_marching_cubes" };
+        if (s.info.num_faces > 0)
+        {
+            if (!verts || !faces)
+                throw ArgError{ TH_ERR_INVALID_ARGUMENT, "verts or faces pointer is NULL" };
+            launch_mc_emit(s.plan, verts, faces, static_cast<cudaStream_t>(stream));
+        }
     });
 }
 

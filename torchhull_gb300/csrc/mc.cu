@@ -1,0 +1,627 @@
+// Public marching cubes over a dense volume or a coalesced sparse COO volume
+// (torchhull marching_cubes: marching_cubes_cuda.cu:376-533 for dense
+// volumes, :535-831 for sparse ones).
+//
+// The reference builds a triangle soup (one vertex per table entry of every
+// active cell, cells ascending, table order inside a cell), keys each soup
+// vertex by its edge id (ravel(lower end point) << 3 | direction, :99-112,
+// direction 1 / 2 / 4 for x / y / z) and sorts the keys with unique_dim; the
+// faces are the soup's inverse indices.  The unique vertices therefore come
+// in edge-id order: by the ravel index of the lower end point, then by axis.
+// Here that order is produced directly: every grid point carries three bits
+// (its +x, +y, +z edge holds a vertex), a scan over the points numbers the
+// set bits, and a face looks up its vertex as the number of set bits before
+// its edge.  The soup order comes from a scan of the per-cell vertex counts,
+// so no sort runs.
+//
+// Which edges hold vertices: every cell's triangulation uses exactly the cell
+// edges whose end points lie on different sides of the isolevel (a property
+// of the table, checked by the tests).  In a dense volume with all sizes >= 2
+// every edge belongs to some cell, so the bits follow from the values alone.
+// In a sparse volume an edge counts only when a complete cell (all 8 corners
+// present) holds it, so each active cell marks its edges on the entries of
+// their lower end points.
+//
+// Axes: x runs along the last volume dimension (W), y along H, z along the
+// first (D).  The reference mixes D and W in its index arithmetic; for
+// volumes with D == W (all of its tests) that mixing is invisible and the
+// results here are identical.
+
+#include <cuda_fp16.h>
+
+#include "mc_tables.h"
+#include "th_internal.h"
+#include "th_mc.cuh"
+
+namespace th
+{
+namespace
+{
+
+__device__ const uint8_t mc_count[256] = TH_MC_TRI_COUNT_INIT;
+__device__ const uint8_t mc_edges[256][15] = TH_MC_TRI_EDGES_INIT;
+
+constexpr unsigned long long kEmptyKey = ~0ull;
+
+// value < isolevel, compared in the value's own type (:166-171, :210-213).
+template <int DT>
+__device__ __forceinline__ bool below(const void* v, int64_t i, float iso)
+{
+    if constexpr (DT == TH_FLOAT64)
+        return static_cast<const double*>(v)[i] < static_cast<double>(iso);
+    else
+        return load_f32<DT>(v, i) < iso;
+}
+
+// interpolate_vertex (:72-97) on the edge from point (x, y, z) along axis,
+// then the optional map to local coordinates: v * 2 / (size - 1) - 1 as two
+// rounded torch operations (:524-531).
+__device__ __forceinline__ void mc_vertex(const McPlan& p, int64_t x, int64_t y, int64_t z, int axis, float v1, float v2, float* out)
+{
+    const float eps = 1e-5f;
+    const int64_t c1[3] = { x, y, z };
+    float q[3];
+    // the reference's check order: snap to p1, to p2, then to p1 again
+    int snap = 0;
+    if (fabsf(__fsub_rn(p.iso, v1)) < eps)
+        snap = 1;
+    else if (fabsf(__fsub_rn(p.iso, v2)) < eps)
+        snap = 2;
+    else if (fabsf(__fsub_rn(v1, v2)) < eps)
+        snap = 1;
+    const float t = snap ? 0.f : __fdiv_rn(__fsub_rn(p.iso, v1), __fsub_rn(v2, v1));
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+        const float f1 = static_cast<float>(c1[a]);
+        const float f2 = static_cast<float>(c1[a] + (a == axis ? 1 : 0));
+        q[a] = snap == 1 ? f1 : (snap == 2 ? f2 : lerp(f1, f2, t));
+        out[a] = p.local ? __fsub_rn(__fmul_rn(q[a], p.scale[a]), 1.f) : q[a];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// dense volumes
+
+template <bool WIDE>
+__device__ __forceinline__ void decode(const McPlan& p, int64_t q, int64_t& x, int64_t& y, int64_t& z)
+{
+    if (WIDE)
+    {
+        const int64_t r = q / p.W;
+        x = q - r * p.W;
+        z = r / p.H;
+        y = r - z * p.H;
+    }
+    else
+    {
+        const uint32_t qq = static_cast<uint32_t>(q), w = static_cast<uint32_t>(p.W), h = static_cast<uint32_t>(p.H);
+        const uint32_t r = qq / w;
+        x = qq - r * w;
+        const uint32_t zz = r / h;
+        z = zz;
+        y = r - zz * h;
+    }
+}
+
+// Edge bits of each group of 32 points (one warp per group).
+template <int DT, bool WIDE>
+__global__ void __launch_bounds__(256) mc_dense_edges_kernel(McPlan p)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    const int64_t WH = p.W * p.H;
+    for (int64_t g = warp; g < p.ngroups; g += nwarps)
+    {
+        const int64_t q = g * 32 + lane;
+        bool ex = false, ey = false, ez = false;
+        if (q < p.points)
+        {
+            int64_t x, y, z;
+            decode<WIDE>(p, q, x, y, z);
+            const bool b = below<DT>(p.volume, q, p.iso);
+            ex = x + 1 < p.W && below<DT>(p.volume, q + 1, p.iso) != b;
+            ey = y + 1 < p.H && below<DT>(p.volume, q + p.W, p.iso) != b;
+            ez = z + 1 < p.D && below<DT>(p.volume, q + WH, p.iso) != b;
+        }
+        const uint32_t X = __ballot_sync(0xffffffffu, ex);
+        const uint32_t Y = __ballot_sync(0xffffffffu, ey);
+        const uint32_t Z = __ballot_sync(0xffffffffu, ez);
+        if (lane == 0)
+            p.groups[g] = McGroup{ X, Y, Z, 0u, 0ull };
+    }
+}
+
+struct GroupCount
+{
+    const McGroup* groups;
+    __device__ unsigned long long operator()(int64_t i) const
+    {
+        const McGroup& e = groups[i];
+        return static_cast<unsigned long long>(__popc(e.x) + __popc(e.y) + __popc(e.z));
+    }
+};
+
+struct GroupEmit
+{
+    McGroup* groups;
+    __device__ void operator()(int64_t i, unsigned long long off, unsigned long long) const
+    {
+        groups[i].base = off;
+    }
+};
+
+struct SoupTotal
+{
+    McCounters* ctr;
+    __device__ void operator()(unsigned long long t) const
+    {
+        ctr->soup = t;
+    }
+};
+
+struct VertTotal
+{
+    McCounters* ctr;
+    __device__ void operator()(unsigned long long t) const
+    {
+        ctr->verts = t;
+    }
+};
+
+// Vertex index of the edge from point q along axis: the set edge bits before it.
+__device__ __forceinline__ unsigned long long dense_vertex(const McGroup* groups, int64_t q, int axis)
+{
+    const McGroup e = groups[q >> 5];
+    const int l = static_cast<int>(q & 31);
+    const uint32_t lt = (1u << l) - 1u;
+    unsigned long long r = e.base + __popc(e.x & lt) + __popc(e.y & lt) + __popc(e.z & lt);
+    if (axis >= 1)
+        r += (e.x >> l) & 1u;
+    if (axis == 2)
+        r += (e.y >> l) & 1u;
+    return r;
+}
+
+// Cell code of the cell with base point q (classify_voxels_dense :146-178),
+// -1 if q is on the last slice of an axis.  Bit i: corner i is below the isolevel.
+template <int DT, bool WIDE>
+__device__ __forceinline__ int dense_code(const McPlan& p, int64_t q, int64_t& x, int64_t& y, int64_t& z)
+{
+    decode<WIDE>(p, q, x, y, z);
+    if (!(x + 1 < p.W && y + 1 < p.H && z + 1 < p.D))
+        return -1;
+    const int64_t WH = p.W * p.H;
+    int code = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+        if (below<DT>(p.volume, q + (i & 1) + ((i >> 1) & 1) * p.W + ((i >> 2) & 1) * WH, p.iso))
+            code |= 1 << i;
+    return code;
+}
+
+template <int DT, bool WIDE>
+struct DenseCellCount
+{
+    McPlan p;
+    __device__ unsigned long long operator()(int64_t q) const
+    {
+        int64_t x, y, z;
+        const int c = dense_code<DT, WIDE>(p, q, x, y, z);
+        return c < 0 ? 0ull : static_cast<unsigned long long>(mc_count[c]);
+    }
+};
+
+// Soup of one active cell (generate_faces_dense :242-306): faces into the
+// unique vertex list, or soup vertices with faces = arange.
+template <int DT, bool WIDE>
+struct DenseCellEmit
+{
+    McPlan p;
+    float* verts;
+    int64_t* faces;
+    __device__ void operator()(int64_t q, unsigned long long off, unsigned long long cnt) const
+    {
+        if (cnt == 0)
+            return;
+        int64_t x, y, z;
+        const int code = dense_code<DT, WIDE>(p, q, x, y, z);
+        const int64_t WH = p.W * p.H;
+        for (int j = 0; j < static_cast<int>(cnt); ++j)
+        {
+            const uint32_t e = mc_edges[code][j];
+            const int lo = static_cast<int>(e & 7u), axis = static_cast<int>(e >> 3);
+            const int64_t q1 = q + (lo & 1) + ((lo >> 1) & 1) * p.W + ((lo >> 2) & 1) * WH;
+            const int64_t k = static_cast<int64_t>(off) + j;
+            if (p.unique)
+            {
+                faces[k] = static_cast<int64_t>(dense_vertex(p.groups, q1, axis));
+            }
+            else
+            {
+                const int64_t q2 = q1 + (axis == 0 ? 1 : (axis == 1 ? p.W : WH));
+                mc_vertex(p, x + (lo & 1), y + ((lo >> 1) & 1), z + ((lo >> 2) & 1), axis, load_f32<DT>(p.volume, q1),
+                          load_f32<DT>(p.volume, q2), verts + 3 * k);
+                faces[k] = k;
+            }
+        }
+    }
+};
+
+// The unique vertices, in edge-id order (one warp per group of 32 points).
+template <int DT, bool WIDE>
+__global__ void __launch_bounds__(256) mc_dense_verts_kernel(McPlan p, float* __restrict__ verts)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    const int64_t WH = p.W * p.H;
+    for (int64_t g = warp; g < p.ngroups; g += nwarps)
+    {
+        const McGroup e = p.groups[g];
+        const uint32_t bit = 1u << lane;
+        const uint32_t mine = ((e.x & bit) ? 1u : 0u) | ((e.y & bit) ? 2u : 0u) | ((e.z & bit) ? 4u : 0u);
+        if (!mine)
+            continue;
+        const uint32_t lt = bit - 1u;
+        unsigned long long r = e.base + __popc(e.x & lt) + __popc(e.y & lt) + __popc(e.z & lt);
+        const int64_t q = g * 32 + lane;
+        int64_t x, y, z;
+        decode<WIDE>(p, q, x, y, z);
+        const float v1 = load_f32<DT>(p.volume, q);
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+        {
+            if (!((mine >> a) & 1u))
+                continue;
+            const int64_t q2 = q + (a == 0 ? 1 : (a == 1 ? p.W : WH));
+            mc_vertex(p, x, y, z, a, v1, load_f32<DT>(p.volume, q2), verts + 3 * r);
+            ++r;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// sparse volumes: an open-addressing table from ravel id to entry index
+// (the reference uses a stdgpu unordered_map, :729-751)
+
+// MurmurHash3's 64-bit finalizer (fmix64).
+__device__ __forceinline__ uint64_t mix64(uint64_t k)
+{
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+
+// Entry t's coordinates, or false when it lies outside the volume.
+__device__ __forceinline__ bool entry_point(const McPlan& p, int64_t t, int64_t& x, int64_t& y, int64_t& z)
+{
+    const int64_t b = p.indices[t];
+    z = p.indices[p.nnz + t];
+    y = p.indices[2 * p.nnz + t];
+    x = p.indices[3 * p.nnz + t];
+    return b == 0 && 0 <= x && x < p.W && 0 <= y && y < p.H && 0 <= z && z < p.D;
+}
+
+__device__ __forceinline__ int32_t mc_find(const McPlan& p, unsigned long long key)
+{
+    uint64_t slot = mix64(key) & p.hmask;
+    for (uint64_t k = 0; k <= p.hmask; ++k)
+    {
+        const unsigned long long kk = p.keys[slot];
+        if (kk == key)
+            return p.slots[slot];
+        if (kk == kEmptyKey)
+            return -1;
+        slot = (slot + 1) & p.hmask;
+    }
+    return -1;
+}
+
+// hash_volume (:114-131): every entry's ravel id into the table; flags
+// entries outside the volume and indices that are not strictly ascending.
+__global__ void __launch_bounds__(256) mc_sparse_insert_kernel(McPlan p)
+{
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < p.nnz; t += stride)
+    {
+        int64_t x, y, z;
+        if (!entry_point(p, t, x, y, z))
+        {
+            atomicOr(&p.ctr->flags, static_cast<unsigned int>(kMcBadIndex));
+            continue;
+        }
+        const unsigned long long key = static_cast<unsigned long long>(x + p.W * (y + p.H * z));
+        if (t > 0)
+        {
+            int64_t px, py, pz;
+            if (entry_point(p, t - 1, px, py, pz) &&
+                static_cast<unsigned long long>(px + p.W * (py + p.H * pz)) >= key)
+                atomicOr(&p.ctr->flags, static_cast<unsigned int>(kMcUnsorted));
+        }
+        uint64_t slot = mix64(key) & p.hmask;
+        for (uint64_t k = 0; k <= p.hmask; ++k)
+        {
+            const unsigned long long prev = atomicCAS(&p.keys[slot], kEmptyKey, key);
+            if (prev == kEmptyKey || prev == key)
+            {
+                p.slots[slot] = static_cast<int32_t>(t);
+                break;
+            }
+            slot = (slot + 1) & p.hmask;
+        }
+    }
+}
+
+// Entry indices of the 8 corners of the cell with base entry t at (x, y, z)
+// (corner i = base + (i & 1, i >> 1 & 1, i >> 2 & 1)); false if one is absent.
+__device__ __forceinline__ bool cell_entries(const McPlan& p, int64_t t, int64_t x, int64_t y, int64_t z, int32_t c[8])
+{
+    if (!(x + 1 < p.W && y + 1 < p.H && z + 1 < p.D))
+        return false;
+    const unsigned long long key = static_cast<unsigned long long>(x + p.W * (y + p.H * z));
+    const unsigned long long WH = static_cast<unsigned long long>(p.W * p.H);
+    c[0] = static_cast<int32_t>(t);
+#pragma unroll
+    for (int i = 1; i < 8; ++i)
+    {
+        c[i] = mc_find(p, key + (i & 1) + ((i >> 1) & 1) * static_cast<unsigned long long>(p.W) + ((i >> 2) & 1) * WH);
+        if (c[i] < 0)
+            return false;
+    }
+    return true;
+}
+
+// classify_voxels_sparse (:180-223) plus, with unique vertices, the marking of
+// the cell's vertex edges on the entries of their lower end points.
+template <int DT>
+__global__ void __launch_bounds__(256) mc_sparse_classify_kernel(McPlan p)
+{
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < p.nnz; t += stride)
+    {
+        int64_t x, y, z;
+        int32_t c[8];
+        int code = 0;
+        if (entry_point(p, t, x, y, z) && cell_entries(p, t, x, y, z, c))
+        {
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (below<DT>(p.values, c[i], p.iso))
+                    code |= 1 << i;
+            if (p.unique && mc_count[code] != 0)
+            {
+                // corner lo owns the edges along the axes where its bit is 0;
+                // an edge is a vertex edge when its two ends differ in the code
+#pragma unroll
+                for (int lo = 0; lo < 8; ++lo)
+                {
+                    uint32_t bits = 0;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a)
+                        if (!((lo >> a) & 1) && (((code >> lo) ^ (code >> (lo | (1 << a)))) & 1))
+                            bits |= 1u << a;
+                    if (bits)
+                        atomicOr(&p.used[c[lo]], bits);
+                }
+            }
+        }
+        p.codes[t] = static_cast<uint8_t>(code);
+    }
+}
+
+struct SparseSoupCount
+{
+    const uint8_t* codes;
+    __device__ unsigned long long operator()(int64_t t) const
+    {
+        return static_cast<unsigned long long>(mc_count[codes[t]]);
+    }
+};
+
+struct SparseVertCount
+{
+    const uint32_t* used;
+    __device__ unsigned long long operator()(int64_t t) const
+    {
+        return static_cast<unsigned long long>(__popc(used[t]));
+    }
+};
+
+struct SparseVertEmit
+{
+    unsigned long long* vbase;
+    __device__ void operator()(int64_t t, unsigned long long off, unsigned long long) const
+    {
+        vbase[t] = off;
+    }
+};
+
+// The unique vertices, in edge-id order (entries are in ravel order).
+template <int DT>
+__global__ void __launch_bounds__(256) mc_sparse_verts_kernel(McPlan p, float* __restrict__ verts)
+{
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const unsigned long long step[3] = { 1ull, static_cast<unsigned long long>(p.W),
+                                         static_cast<unsigned long long>(p.W * p.H) };
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < p.nnz; t += stride)
+    {
+        const uint32_t bits = p.used[t];
+        if (!bits)
+            continue;
+        int64_t x, y, z;
+        entry_point(p, t, x, y, z);
+        const unsigned long long key = static_cast<unsigned long long>(x + p.W * (y + p.H * z));
+        const float v1 = load_f32<DT>(p.values, t);
+        unsigned long long r = p.vbase[t];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+        {
+            if (!((bits >> a) & 1u))
+                continue;
+            // present: a complete cell holds this edge
+            const int32_t t2 = mc_find(p, key + step[a]);
+            const float v2 = t2 >= 0 ? load_f32<DT>(p.values, t2) : __int_as_float(0x7fffffff);
+            mc_vertex(p, x, y, z, a, v1, v2, verts + 3 * r);
+            ++r;
+        }
+    }
+}
+
+// Soup of one active entry (generate_faces_sparse :308-374).
+template <int DT>
+struct SparseCellEmit
+{
+    McPlan p;
+    float* verts;
+    int64_t* faces;
+    __device__ void operator()(int64_t t, unsigned long long off, unsigned long long cnt) const
+    {
+        if (cnt == 0)
+            return;
+        int64_t x, y, z;
+        int32_t c[8];
+        entry_point(p, t, x, y, z);
+        if (!cell_entries(p, t, x, y, z, c))
+            return; // not reached: an entry with a count has all its corners
+        const int code = p.codes[t];
+        for (int j = 0; j < static_cast<int>(cnt); ++j)
+        {
+            const uint32_t e = mc_edges[code][j];
+            const int lo = static_cast<int>(e & 7u), axis = static_cast<int>(e >> 3);
+            const int64_t k = static_cast<int64_t>(off) + j;
+            const int32_t c1 = c[lo];
+            if (p.unique)
+            {
+                faces[k] = static_cast<int64_t>(p.vbase[c1] + __popc(p.used[c1] & ((1u << axis) - 1u)));
+            }
+            else
+            {
+                const int32_t c2 = c[lo | (1 << axis)];
+                mc_vertex(p, x + (lo & 1), y + ((lo >> 1) & 1), z + ((lo >> 2) & 1), axis, load_f32<DT>(p.values, c1),
+                          load_f32<DT>(p.values, c2), verts + 3 * k);
+                faces[k] = k;
+            }
+        }
+    }
+};
+
+template <int DT, bool WIDE>
+void dense_count(const McPlan& p, cudaStream_t s)
+{
+    if (p.unique)
+    {
+        mc_dense_edges_kernel<DT, WIDE><<<grid_for(p.ngroups * 32, 256), 256, 0, s>>>(p);
+        TH_LAUNCH_CHECK();
+        run_scan(GroupCount{ p.groups }, GroupEmit{ p.groups }, VertTotal{ p.ctr }, Count{ nullptr, p.ngroups },
+                 p.ngroups, p.tiles_verts, &p.ctr->scan_verts, s);
+    }
+    run_scan_reduce(DenseCellCount<DT, WIDE>{ p }, SoupTotal{ p.ctr }, Count{ nullptr, p.points }, p.points,
+                    p.tiles_soup, &p.ctr->scan_soup, s);
+}
+
+template <int DT, bool WIDE>
+void dense_emit(const McPlan& p, float* verts, int64_t* faces, cudaStream_t s)
+{
+    if (p.unique)
+    {
+        mc_dense_verts_kernel<DT, WIDE><<<grid_for(p.ngroups * 32, 256), 256, 0, s>>>(p, verts);
+        TH_LAUNCH_CHECK();
+    }
+    run_scan_apply(DenseCellCount<DT, WIDE>{ p }, DenseCellEmit<DT, WIDE>{ p, verts, faces },
+                   Count{ nullptr, p.points }, p.points, p.tiles_soup, s);
+}
+
+template <int DT>
+void sparse_count(const McPlan& p, cudaStream_t s)
+{
+    const int grid = grid_for(p.nnz, 256);
+    mc_sparse_insert_kernel<<<grid, 256, 0, s>>>(p);
+    TH_LAUNCH_CHECK();
+    mc_sparse_classify_kernel<DT><<<grid, 256, 0, s>>>(p);
+    TH_LAUNCH_CHECK();
+    run_scan_reduce(SparseSoupCount{ p.codes }, SoupTotal{ p.ctr }, Count{ nullptr, p.nnz }, p.nnz, p.tiles_soup,
+                    &p.ctr->scan_soup, s);
+    if (p.unique)
+        run_scan(SparseVertCount{ p.used }, SparseVertEmit{ p.vbase }, VertTotal{ p.ctr }, Count{ nullptr, p.nnz },
+                 p.nnz, p.tiles_verts, &p.ctr->scan_verts, s);
+}
+
+template <int DT>
+void sparse_emit(const McPlan& p, float* verts, int64_t* faces, cudaStream_t s)
+{
+    if (p.unique)
+    {
+        mc_sparse_verts_kernel<DT><<<grid_for(p.nnz, 256), 256, 0, s>>>(p, verts);
+        TH_LAUNCH_CHECK();
+    }
+    run_scan_apply(SparseSoupCount{ p.codes }, SparseCellEmit<DT>{ p, verts, faces }, Count{ nullptr, p.nnz }, p.nnz,
+                   p.tiles_soup, s);
+}
+
+template <class F>
+void dispatch_value_dtype(int dt, F&& f)
+{
+    switch (dt)
+    {
+    case TH_FLOAT16:
+        f.template operator()<TH_FLOAT16>();
+        break;
+    case TH_FLOAT32:
+        f.template operator()<TH_FLOAT32>();
+        break;
+    default:
+        f.template operator()<TH_FLOAT64>();
+        break;
+    }
+}
+
+} // namespace
+
+void launch_mc_count(const McPlan& p, cudaStream_t s)
+{
+    TH_CUDA(cudaMemsetAsync(p.ctr, 0, sizeof(McCounters), s));
+    if (p.sparse)
+    {
+        if (p.nnz == 0)
+            return;
+        TH_CUDA(cudaMemsetAsync(p.keys, 0xff, sizeof(unsigned long long) * (p.hmask + 1), s));
+        if (p.unique)
+            TH_CUDA(cudaMemsetAsync(p.used, 0, sizeof(uint32_t) * p.nnz, s));
+        dispatch_value_dtype(p.dtype, [&]<int DT>() { sparse_count<DT>(p, s); });
+        return;
+    }
+    if (p.points == 0)
+        return;
+    dispatch_value_dtype(p.dtype, [&]<int DT>() {
+        if (p.wide)
+            dense_count<DT, true>(p, s);
+        else
+            dense_count<DT, false>(p, s);
+    });
+}
+
+void launch_mc_emit(const McPlan& p, float* verts, int64_t* faces, cudaStream_t s)
+{
+    if (p.sparse)
+    {
+        if (p.nnz == 0)
+            return;
+        dispatch_value_dtype(p.dtype, [&]<int DT>() { sparse_emit<DT>(p, verts, faces, s); });
+        return;
+    }
+    if (p.points == 0)
+        return;
+    dispatch_value_dtype(p.dtype, [&]<int DT>() {
+        if (p.wide)
+            dense_emit<DT, true>(p, verts, faces, s);
+        else
+            dense_emit<DT, false>(p, verts, faces, s);
+    });
+}
+
+} // namespace th

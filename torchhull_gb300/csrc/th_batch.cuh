@@ -47,6 +47,8 @@ struct BatchPlan
     uint32_t* node_skip;
     int64_t node_cap;
     BatchCounters* ctr;
+    // (partial << 1) | opengl when every request shares it, -1 otherwise
+    int32_t variant;
 };
 
 void launch_batch_init(const BatchPlan& bp, cudaStream_t s);

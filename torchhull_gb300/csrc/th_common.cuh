@@ -376,8 +376,41 @@ int sm_count();
 void note_launches(int n);
 void check_launch(const char* what);
 
-// Both scan passes on stream s.  n_max bounds the item count on the host side
-// (it sizes the grid; tile_sums must hold ceil(n_max / kScanTile) entries).
+inline int scan_grid(int64_t n_max)
+{
+    const int64_t tiles = (n_max + kScanTile - 1) / kScanTile;
+    const int64_t cap = 4LL * sm_count();
+    return static_cast<int>(tiles < 1 ? 1 : (tiles < cap ? tiles : cap));
+}
+
+// Pass 1 on stream s: tile sums, then exclusive tile offsets in tile_sums and
+// epi(total).  n_max bounds the item count on the host side (it sizes the
+// grid; tile_sums must hold ceil(n_max / kScanTile) entries).
+template <class CountF, class EpiF>
+inline void run_scan_reduce(CountF count,
+                            EpiF epi,
+                            Count n,
+                            int64_t n_max,
+                            unsigned long long* tile_sums,
+                            ScanState* state,
+                            cudaStream_t s)
+{
+    scan_reduce_kernel<<<scan_grid(n_max), kScanThreads, 0, s>>>(count, n, tile_sums, state, epi);
+    check_launch("device-wide scan (reduce)");
+    note_launches(1);
+}
+
+// Pass 2 on stream s, after run_scan_reduce over the same items: emit(i,
+// offset, count) for every item.
+template <class CountF, class EmitF>
+inline void run_scan_apply(CountF count, EmitF emit, Count n, int64_t n_max, const unsigned long long* tile_sums, cudaStream_t s)
+{
+    scan_apply_kernel<<<scan_grid(n_max), kScanThreads, 0, s>>>(count, emit, n, tile_sums);
+    check_launch("device-wide scan (apply)");
+    note_launches(1);
+}
+
+// Both scan passes on stream s.
 template <class CountF, class EmitF, class EpiF>
 inline void run_scan(CountF count,
                      EmitF emit,
@@ -388,13 +421,8 @@ inline void run_scan(CountF count,
                      ScanState* state,
                      cudaStream_t s)
 {
-    const int64_t tiles = (n_max + kScanTile - 1) / kScanTile;
-    const int64_t cap = 4LL * sm_count();
-    const int grid = static_cast<int>(tiles < 1 ? 1 : (tiles < cap ? tiles : cap));
-    scan_reduce_kernel<<<grid, kScanThreads, 0, s>>>(count, n, tile_sums, state, epi);
-    scan_apply_kernel<<<grid, kScanThreads, 0, s>>>(count, emit, n, tile_sums);
-    check_launch("device-wide scan");
-    note_launches(2);
+    run_scan_reduce(count, epi, n, n_max, tile_sums, state, s);
+    run_scan_apply(count, emit, n, n_max, tile_sums, s);
 }
 
 } // namespace th

@@ -261,6 +261,65 @@ at::Tensor gaussian_blur(const at::Tensor& images_in,
     return out;
 }
 
+// torchhull::marching_cubes (marching_cubes.cpp:19-31; the tensor checks of
+// marching_cubes_cuda.cu:382-385 for dense volumes and :789-795 for sparse
+// ones, in the reference's order).
+std::tuple<at::Tensor, at::Tensor> marching_cubes(const at::Tensor& volume,
+                                                  float isolevel,
+                                                  bool return_local_coords,
+                                                  bool unique_verts)
+{
+    require_cuda(volume);
+    at::cuda::CUDAGuard guard(volume.device());
+    th_mc_args a{};
+    at::Tensor dense, indices, values;
+    if (volume.is_sparse())
+    {
+        TORCH_CHECK_EQ(volume.size(0), 1);
+        TORCH_CHECK_LE(volume.numel(), (static_cast<int64_t>(1) << 60));
+        TORCH_CHECK_EQ(volume.layout(), torch::Layout::Sparse);
+        TORCH_CHECK_EQ(volume.sparse_dim(), 4);
+        TORCH_CHECK_EQ(volume.dense_dim(), 0);
+        TORCH_CHECK_LT(volume.values().numel(), (static_cast<int64_t>(1) << 31)); // stdgpu uses 32-bit indices
+        TORCH_CHECK_GE(isolevel, 0);
+        indices = volume.indices().contiguous();
+        values = volume.values().contiguous();
+        a.sparse = 1;
+        a.dtype = th_dtype_of(values.scalar_type());
+        a.indices = indices.data_ptr<int64_t>();
+        a.values = values.data_ptr();
+        a.nnz = values.numel();
+    }
+    else
+    {
+        TORCH_CHECK_EQ(volume.dim(), 4);
+        TORCH_CHECK_EQ(volume.size(0), 1);
+        TORCH_CHECK_LE(volume.numel(), (static_cast<int64_t>(1) << 60));
+        TORCH_CHECK_GE(isolevel, 0);
+        dense = volume.contiguous();
+        a.sparse = 0;
+        a.dtype = th_dtype_of(dense.scalar_type());
+        a.volume = dense.data_ptr();
+    }
+    a.depth = volume.size(1);
+    a.height = volume.size(2);
+    a.width = volume.size(3);
+    a.isolevel = isolevel;
+    a.return_local_coords = return_local_coords ? 1 : 0;
+    a.unique_verts = unique_verts ? 1 : 0;
+
+    DeviceContext& dc = context_for(volume.device().index());
+    std::lock_guard<std::mutex> g(dc.lock);
+    void* stream = stream_of(volume);
+    th_mc_info info{};
+    check(th_marching_cubes(dc.ctx, &a, stream, &info), dc.ctx);
+    const auto dev = volume.device();
+    at::Tensor verts = at::empty({ info.num_verts, 3 }, at::TensorOptions().dtype(at::kFloat).device(dev));
+    at::Tensor faces = at::empty({ info.num_faces, 3 }, at::TensorOptions().dtype(at::kLong).device(dev));
+    check(th_marching_cubes_export(dc.ctx, verts.data_ptr<float>(), faces.data_ptr<int64_t>(), stream), dc.ctx);
+    return { verts, faces };
+}
+
 at::Tensor integral_image(const at::Tensor& masks_in)
 {
     require_cuda(masks_in);
@@ -459,6 +518,10 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
           "Sparse hull field as (ravelled indices, values, grid size).");
     m.def("gaussian_blur", &gaussian_blur, "images"_a, "kernel_size"_a, "sigma"_a, "sparse"_a = true,
           "dtype"_a = pybind11::none(), "Gaussian blur of [B,H,W,1] images.");
+    m.def("marching_cubes", &marching_cubes, "volume"_a, "isolevel"_a, "return_local_coords"_a = true,
+          "unique_verts"_a = true,
+          "Marching Cubes on a 1 x D x H x W dense or sparse COO volume; returns (verts [V,3] float32, "
+          "faces [F,3] int64).");
     m.def("integral_image", &integral_image, "masks"_a, "Float32 integral image [B,H,W] of masks [B,H,W,1].");
     m.def("device_pool_bytes", &device_pool_bytes, "device"_a, "Bytes held by the device's resident pools.");
     m.def("set_profiling", &set_profiling, "device"_a, "enable"_a, "Record CUDA events between hull stages.");
