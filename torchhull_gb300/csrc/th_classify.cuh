@@ -132,6 +132,10 @@ __device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sa
     return res;
 }
 
+#ifndef TH_CARVE_ROLL_Z
+#define TH_CARVE_ROLL_Z 0
+#endif
+
 struct ItemResult
 {
     uint32_t empty, refine, inside, skip; // 8-bit child masks
@@ -245,12 +249,19 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
     ItemResult out{ 0, 0, 0, 0 };
     Box prev[4];
     uint32_t prev_in = 0, prev_in2 = 0, prev_front = 0;
+    // Rolled, the plane loop keeps one copy of the plane's code (a third of
+    // the instruction footprint); unrolled, it schedules across planes.
+#if TH_CARVE_ROLL_Z
+#pragma unroll 1
+#else
 #pragma unroll
+#endif
     for (int z = 0; z < 3; ++z)
     {
-        const float tzx = __fmaf_rn(rx.z, wz[z], rx.w);
-        const float tzy = __fmaf_rn(ry.z, wz[z], ry.w);
-        const float tzd = __fmaf_rn(rd.z, wz[z], rd.w);
+        const float wzz = z == 0 ? wz[0] : (z == 1 ? wz[1] : wz[2]);
+        const float tzx = __fmaf_rn(rx.z, wzz, rx.w);
+        const float tzy = __fmaf_rn(ry.z, wzz, ry.w);
+        const float tzd = __fmaf_rn(rd.z, wzz, rd.w);
         float px[9], py[9];
         uint32_t in9 = 0, in9b = 0, front9 = 0;
 #pragma unroll

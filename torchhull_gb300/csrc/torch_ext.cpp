@@ -22,6 +22,18 @@
 
 #include "../../include/torchhull_gb300.h"
 
+// The reference's TORCH_CHECK_EQ/LE/... checks, with their message
+// ("Check failed: a op b (x vs. y). "), raised as RuntimeError on every torch
+// version: some versions abort the process on a failed TORCH_CHECK_OP.
+#define TH_CHECK_OP(a, b, op) \
+    TORCH_CHECK((a)op(b), "Check failed: " #a " " #op " " #b " (", (a), " vs. ", (b), "). ")
+#define TH_CHECK_EQ(a, b) TH_CHECK_OP(a, b, ==)
+#define TH_CHECK_NE(a, b) TH_CHECK_OP(a, b, !=)
+#define TH_CHECK_LE(a, b) TH_CHECK_OP(a, b, <=)
+#define TH_CHECK_LT(a, b) TH_CHECK_OP(a, b, <)
+#define TH_CHECK_GE(a, b) TH_CHECK_OP(a, b, >=)
+#define TH_CHECK_GT(a, b) TH_CHECK_OP(a, b, >)
+
 namespace
 {
 
@@ -103,15 +115,15 @@ th_hull_args hull_args(const at::Tensor& masks,
                        bool unique_verts)
 {
     // visual_hull_cuda.cu:591-613
-    TORCH_CHECK_EQ(masks.device(), transforms.device());
-    TORCH_CHECK_EQ(masks.dim(), 4);
-    TORCH_CHECK_EQ(transforms.dim(), 3);
-    TORCH_CHECK_EQ(transforms.size(1), 4);
-    TORCH_CHECK_EQ(transforms.size(2), 4);
-    TORCH_CHECK_EQ(masks.size(0), transforms.size(0));
-    TORCH_CHECK_EQ(masks.size(3), 1);
-    TORCH_CHECK_GE(level, 0);
-    TORCH_CHECK_GT(cube_length, 0.f);
+    TH_CHECK_EQ(masks.device(), transforms.device());
+    TH_CHECK_EQ(masks.dim(), 4);
+    TH_CHECK_EQ(transforms.dim(), 3);
+    TH_CHECK_EQ(transforms.size(1), 4);
+    TH_CHECK_EQ(transforms.size(2), 4);
+    TH_CHECK_EQ(masks.size(0), transforms.size(0));
+    TH_CHECK_EQ(masks.size(3), 1);
+    TH_CHECK_GE(level, 0);
+    TH_CHECK_GT(cube_length, 0.f);
     bool opengl = false;
     if (transforms_convention == "opengl")
         opengl = true;
@@ -247,8 +259,8 @@ at::Tensor gaussian_blur(const at::Tensor& images_in,
 {
     require_cuda(images_in);
     at::cuda::CUDAGuard guard(images_in.device());
-    TORCH_CHECK_EQ(images_in.dim(), 4);
-    TORCH_CHECK_EQ(images_in.size(3), 1);
+    TH_CHECK_EQ(images_in.dim(), 4);
+    TH_CHECK_EQ(images_in.size(3), 1);
     const at::Tensor images = images_in.contiguous();
     const at::ScalarType out_type = dtype.value_or(images.scalar_type());
     at::Tensor out = at::empty(images.sizes(), images.options().dtype(out_type));
@@ -275,13 +287,13 @@ std::tuple<at::Tensor, at::Tensor> marching_cubes(const at::Tensor& volume,
     at::Tensor dense, indices, values;
     if (volume.is_sparse())
     {
-        TORCH_CHECK_EQ(volume.size(0), 1);
-        TORCH_CHECK_LE(volume.numel(), (static_cast<int64_t>(1) << 60));
-        TORCH_CHECK_EQ(volume.layout(), torch::Layout::Sparse);
-        TORCH_CHECK_EQ(volume.sparse_dim(), 4);
-        TORCH_CHECK_EQ(volume.dense_dim(), 0);
-        TORCH_CHECK_LT(volume.values().numel(), (static_cast<int64_t>(1) << 31)); // stdgpu uses 32-bit indices
-        TORCH_CHECK_GE(isolevel, 0);
+        TH_CHECK_EQ(volume.size(0), 1);
+        TH_CHECK_LE(volume.numel(), (static_cast<int64_t>(1) << 60));
+        TH_CHECK_EQ(volume.layout(), torch::Layout::Sparse);
+        TH_CHECK_EQ(volume.sparse_dim(), 4);
+        TH_CHECK_EQ(volume.dense_dim(), 0);
+        TH_CHECK_LT(volume.values().numel(), (static_cast<int64_t>(1) << 31)); // stdgpu uses 32-bit indices
+        TH_CHECK_GE(isolevel, 0);
         indices = volume.indices().contiguous();
         values = volume.values().contiguous();
         a.sparse = 1;
@@ -292,10 +304,10 @@ std::tuple<at::Tensor, at::Tensor> marching_cubes(const at::Tensor& volume,
     }
     else
     {
-        TORCH_CHECK_EQ(volume.dim(), 4);
-        TORCH_CHECK_EQ(volume.size(0), 1);
-        TORCH_CHECK_LE(volume.numel(), (static_cast<int64_t>(1) << 60));
-        TORCH_CHECK_GE(isolevel, 0);
+        TH_CHECK_EQ(volume.dim(), 4);
+        TH_CHECK_EQ(volume.size(0), 1);
+        TH_CHECK_LE(volume.numel(), (static_cast<int64_t>(1) << 60));
+        TH_CHECK_GE(isolevel, 0);
         dense = volume.contiguous();
         a.sparse = 0;
         a.dtype = th_dtype_of(dense.scalar_type());
@@ -324,7 +336,7 @@ at::Tensor integral_image(const at::Tensor& masks_in)
 {
     require_cuda(masks_in);
     at::cuda::CUDAGuard guard(masks_in.device());
-    TORCH_CHECK_EQ(masks_in.dim(), 4);
+    TH_CHECK_EQ(masks_in.dim(), 4);
     const at::Tensor masks = masks_in.contiguous();
     at::Tensor out = at::empty({ masks.size(0), masks.size(1), masks.size(2) }, masks.options().dtype(at::kFloat));
     DeviceContext& dc = context_for(masks.device().index());
