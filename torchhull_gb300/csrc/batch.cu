@@ -77,7 +77,7 @@ __device__ __forceinline__ int64_t level_entries(const BatchPlan& bp, int li, in
 }
 
 template <int VARIANT>
-__global__ void __launch_bounds__(32 * kBatchWarps) batch_carve_kernel(BatchPlan bp)
+__global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchPlan bp)
 {
     cg::grid_group grid = cg::this_grid();
     __shared__ WarpSlots slots_all[kBatchWarps];
@@ -189,6 +189,21 @@ __global__ void __launch_bounds__(32 * kBatchWarps) batch_carve_kernel(BatchPlan
                 obase = atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->count[li + 1]),
                                   static_cast<unsigned long long>(ctot));
             obase = __shfl_sync(0xffffffffu, obase, 0);
+            // children per request: one atomic when the chunk is one request's
+            {
+                unsigned long long* rc = bp.req_count + static_cast<int64_t>(li + 1) * bp.nreq;
+                const int rq = static_cast<int>(node >> kTagShift);
+                const int r0 = __shfl_sync(0xffffffffu, rq, 0);
+                if (__all_sync(0xffffffffu, nch == 0 || rq == r0))
+                {
+                    if (lane == 0 && ctot > 0)
+                        atomicAdd(&rc[r0], static_cast<unsigned long long>(ctot));
+                }
+                else if (nch)
+                {
+                    atomicAdd(&rc[rq], static_cast<unsigned long long>(nch));
+                }
+            }
             if (nch)
             {
                 const bool produce_me = skips && (li + 1 < q.level);
@@ -197,17 +212,17 @@ __global__ void __launch_bounds__(32 * kBatchWarps) batch_carve_kernel(BatchPlan
                 const int64_t gx = 2 * (cell & m), gy = 2 * ((cell >> li) & m), gz = 2 * (cell >> (2 * li));
                 const int sh = li + 1;
                 const int64_t tag = node & ~kCellMask;
-                int64_t out = next + static_cast<int64_t>(obase) + (cincl - nch);
+                int64_t out = static_cast<int64_t>(obase) + (cincl - nch);
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
                 {
                     if (!(mask >> c & 1u))
                         continue;
-                    if (out < bp.node_cap)
+                    if (next + out < bp.node_cap)
                     {
-                        bp.nodes[out] = tag | (gx + (c & 1)) | ((gy + (c >> 1 & 1)) << sh) |
-                                        ((gz + (c >> 2 & 1)) << (2 * sh));
-                        bp.node_skip[out] = produce_me ? ws.cskip[lane][c] : 0u;
+                        bp.stage_nodes[out] = tag | (gx + (c & 1)) | ((gy + (c >> 1 & 1)) << sh) |
+                                              ((gz + (c >> 2 & 1)) << (2 * sh));
+                        bp.stage_skip[out] = produce_me ? ws.cskip[lane][c] : 0u;
                     }
                     else
                         atomicOr(&ctr->overflow, 1ull);
@@ -215,6 +230,52 @@ __global__ void __launch_bounds__(32 * kBatchWarps) batch_carve_kernel(BatchPlan
                 }
             }
             __syncwarp();
+        }
+        grid.sync();
+        // the children into the pool, grouped by request (order inside a
+        // request: warp chunks as they were appended)
+        const int64_t nc = level_entries(bp, li + 1, next);
+        unsigned long long* rc = bp.req_count + static_cast<int64_t>(li + 1) * bp.nreq;
+        unsigned long long* cur = bp.req_cursor + static_cast<int64_t>(li + 1) * bp.nreq;
+        if (blockIdx.x == 0 && threadIdx.x < 32)
+        {
+            unsigned long long carry = static_cast<unsigned long long>(next);
+            for (int r0 = 0; r0 < bp.nreq; r0 += 32)
+            {
+                const int r = r0 + lane;
+                const unsigned long long v = r < bp.nreq ? rc[r] : 0ull;
+                const unsigned long long inc = warp_inclusive_scan(v);
+                if (r < bp.nreq)
+                    cur[r] = carry + inc - v;
+                carry += __shfl_sync(0xffffffffu, inc, 31);
+            }
+        }
+        grid.sync();
+        const int64_t warp_id = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+        for (int64_t b0 = warp_id * 32; b0 < nc; b0 += nwarps * 32)
+        {
+            const int64_t i = b0 + lane;
+            const bool ok = i < nc;
+            const int64_t nd = ok ? bp.stage_nodes[i] : 0;
+            const uint32_t sk = ok ? bp.stage_skip[i] : 0u;
+            const int rq = ok ? static_cast<int>(nd >> kTagShift) : -1;
+            const unsigned grp = __match_any_sync(0xffffffffu, rq);
+            const int leader = __ffs(grp) - 1;
+            unsigned long long pos = 0;
+            if (ok && lane == leader)
+                pos = atomicAdd(&cur[rq], static_cast<unsigned long long>(__popc(grp)));
+            pos = __shfl_sync(0xffffffffu, pos, leader) + __popc(grp & ((1u << lane) - 1u));
+            if (ok)
+            {
+                // children dropped by an overflow still count in the cursors
+                if (pos < static_cast<unsigned long long>(bp.node_cap))
+                {
+                    bp.nodes[pos] = nd;
+                    bp.node_skip[pos] = sk;
+                }
+                else
+                    atomicOr(&ctr->overflow, 1ull);
+            }
         }
         grid.sync();
         start = next;
@@ -252,6 +313,7 @@ __global__ void __launch_bounds__(256) batch_mark_kernel(BatchPlan bp)
 void launch_batch_init(const BatchPlan& bp, cudaStream_t s)
 {
     TH_CUDA(cudaMemsetAsync(bp.ctr, 0, sizeof(BatchCounters), s));
+    TH_CUDA(cudaMemsetAsync(bp.req_count, 0, sizeof(unsigned long long) * (kMaxLevel + 2) * bp.nreq, s));
     batch_init_kernel<<<1, 256, 0, s>>>(bp);
     TH_LAUNCH_CHECK();
 }

@@ -233,7 +233,7 @@ namespace
 // carve, the request table, and the streams the per-request stages run on.
 struct BatchState
 {
-    DevBuf reqs, nodes, node_skip, ctr;
+    DevBuf reqs, nodes, node_skip, ctr, stage_nodes, stage_skip, req_work;
     BatchReq* host_reqs = nullptr; // pinned
     int32_t host_reqs_cap = 0;
     BatchCounters* host_ctr = nullptr; // pinned
@@ -244,7 +244,7 @@ struct BatchState
 
     void release()
     {
-        for (DevBuf* b : { &reqs, &nodes, &node_skip, &ctr })
+        for (DevBuf* b : { &reqs, &nodes, &node_skip, &ctr, &stage_nodes, &stage_skip, &req_work })
             b->release();
         if (host_reqs)
             cudaFreeHost(host_reqs);
@@ -702,6 +702,9 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
         bs.reqs.ensure(sizeof(BatchReq) * n);
         bs.nodes.ensure(sizeof(int64_t) * bs.node_cap);
         bs.node_skip.ensure(sizeof(uint32_t) * bs.node_cap);
+        bs.stage_nodes.ensure(sizeof(int64_t) * bs.node_cap);
+        bs.stage_skip.ensure(sizeof(uint32_t) * bs.node_cap);
+        bs.req_work.ensure(sizeof(unsigned long long) * 2 * (kMaxLevel + 2) * n);
         bs.ctr.ensure(sizeof(BatchCounters));
         for (int32_t r = 0; r < n; ++r)
         {
@@ -749,6 +752,10 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
         bp.node_skip = bs.node_skip.as<uint32_t>();
         bp.node_cap = bs.node_cap;
         bp.ctr = bs.ctr.as<BatchCounters>();
+        bp.stage_nodes = bs.stage_nodes.as<int64_t>();
+        bp.stage_skip = bs.stage_skip.as<uint32_t>();
+        bp.req_count = bs.req_work.as<unsigned long long>();
+        bp.req_cursor = bp.req_count + (kMaxLevel + 2) * n;
         bp.variant = -1;
         for (int32_t r = 0; r < n; ++r)
         {
