@@ -972,7 +972,9 @@ void run_mc(McSlot& s, const th_mc_args* a, cudaStream_t st)
     else
     {
         s.tiles_soup.ensure(sizeof(unsigned long long) * mc_scan_tiles(p.points));
+        s.codes.ensure(static_cast<size_t>(p.points));
         p.tiles_soup = s.tiles_soup.as<unsigned long long>();
+        p.codes = s.codes.as<uint8_t>();
         if (p.unique)
         {
             s.groups.ensure(sizeof(McGroup) * p.ngroups);

@@ -201,53 +201,89 @@ __device__ __forceinline__ int dense_code(const McPlan& p, int64_t q, int64_t& x
     return code;
 }
 
+// Soup of the active cell with base point q and code (generate_faces_dense
+// :242-306): faces into the unique vertex list, or soup vertices with
+// faces = arange.  off: the cell's first soup vertex.
 template <int DT, bool WIDE>
-struct DenseCellCount
+__device__ __forceinline__ void dense_emit_cell(const McPlan& p, int64_t q, int code, unsigned long long off, int cnt, float* verts, int64_t* faces)
 {
-    McPlan p;
-    __device__ unsigned long long operator()(int64_t q) const
+    int64_t x, y, z;
+    decode<WIDE>(p, q, x, y, z);
+    const int64_t WH = p.W * p.H;
+    for (int j = 0; j < cnt; ++j)
     {
-        int64_t x, y, z;
-        const int c = dense_code<DT, WIDE>(p, q, x, y, z);
-        return c < 0 ? 0ull : static_cast<unsigned long long>(mc_count[c]);
-    }
-};
-
-// Soup of one active cell (generate_faces_dense :242-306): faces into the
-// unique vertex list, or soup vertices with faces = arange.
-template <int DT, bool WIDE>
-struct DenseCellEmit
-{
-    McPlan p;
-    float* verts;
-    int64_t* faces;
-    __device__ void operator()(int64_t q, unsigned long long off, unsigned long long cnt) const
-    {
-        if (cnt == 0)
-            return;
-        int64_t x, y, z;
-        const int code = dense_code<DT, WIDE>(p, q, x, y, z);
-        const int64_t WH = p.W * p.H;
-        for (int j = 0; j < static_cast<int>(cnt); ++j)
+        const uint32_t e = mc_edges[code][j];
+        const int lo = static_cast<int>(e & 7u), axis = static_cast<int>(e >> 3);
+        const int64_t q1 = q + (lo & 1) + ((lo >> 1) & 1) * p.W + ((lo >> 2) & 1) * WH;
+        const int64_t k = static_cast<int64_t>(off) + j;
+        if (p.unique)
         {
-            const uint32_t e = mc_edges[code][j];
-            const int lo = static_cast<int>(e & 7u), axis = static_cast<int>(e >> 3);
-            const int64_t q1 = q + (lo & 1) + ((lo >> 1) & 1) * p.W + ((lo >> 2) & 1) * WH;
-            const int64_t k = static_cast<int64_t>(off) + j;
-            if (p.unique)
-            {
-                faces[k] = static_cast<int64_t>(dense_vertex(p.groups, q1, axis));
-            }
-            else
-            {
-                const int64_t q2 = q1 + (axis == 0 ? 1 : (axis == 1 ? p.W : WH));
-                mc_vertex(p, x + (lo & 1), y + ((lo >> 1) & 1), z + ((lo >> 2) & 1), axis, load_f32<DT>(p.volume, q1),
-                          load_f32<DT>(p.volume, q2), verts + 3 * k);
-                faces[k] = k;
-            }
+            faces[k] = static_cast<int64_t>(dense_vertex(p.groups, q1, axis));
+        }
+        else
+        {
+            const int64_t q2 = q1 + (axis == 0 ? 1 : (axis == 1 ? p.W : WH));
+            mc_vertex(p, x + (lo & 1), y + ((lo >> 1) & 1), z + ((lo >> 2) & 1), axis, load_f32<DT>(p.volume, q1),
+                      load_f32<DT>(p.volume, q2), verts + 3 * k);
+            faces[k] = k;
         }
     }
-};
+}
+
+// Pass 1 over the points in tiles of kScanTile, each tile in kScanItems
+// rounds of kScanThreads consecutive points (coalesced corner loads): the
+// cell code of every point into codes[] (0 where no cell starts), the soup
+// vertex count of every tile into tiles_soup, then exclusive tile offsets.
+template <int DT, bool WIDE>
+__global__ void __launch_bounds__(kScanThreads) mc_dense_codes_kernel(McPlan p)
+{
+    const int64_t ntiles = (p.points + kScanTile - 1) / kScanTile;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+    {
+        unsigned long long s = 0;
+#pragma unroll 2
+        for (int k = 0; k < kScanItems; ++k)
+        {
+            const int64_t q = tile * kScanTile + k * kScanThreads + threadIdx.x;
+            if (q < p.points)
+            {
+                int64_t x, y, z;
+                const int c = dense_code<DT, WIDE>(p, q, x, y, z);
+                const int code = c < 0 ? 0 : c;
+                p.codes[q] = static_cast<uint8_t>(code);
+                s += mc_count[code];
+            }
+        }
+        unsigned long long tot;
+        block_exclusive_scan(s, &tot);
+        if (threadIdx.x == 0)
+            p.tiles_soup[tile] = tot;
+    }
+    finish_tile_sums(ntiles, p.tiles_soup, &p.ctr->scan_soup, SoupTotal{ p.ctr });
+}
+
+// Pass 2: the same rounds, each one block scan of the counts, then the
+// active cells' soup.
+template <int DT, bool WIDE>
+__global__ void __launch_bounds__(kScanThreads) mc_dense_emit_kernel(McPlan p, float* __restrict__ verts, int64_t* __restrict__ faces)
+{
+    const int64_t ntiles = (p.points + kScanTile - 1) / kScanTile;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+    {
+        unsigned long long off = p.tiles_soup[tile];
+        for (int k = 0; k < kScanItems; ++k)
+        {
+            const int64_t q = tile * kScanTile + k * kScanThreads + threadIdx.x;
+            const int code = q < p.points ? p.codes[q] : 0;
+            const int cnt = mc_count[code];
+            unsigned long long tot;
+            const unsigned long long ex = block_exclusive_scan(static_cast<unsigned long long>(cnt), &tot);
+            if (cnt)
+                dense_emit_cell<DT, WIDE>(p, q, code, off + ex, cnt, verts, faces);
+            off += tot;
+        }
+    }
+}
 
 // The unique vertices, in edge-id order (one warp per group of 32 points).
 template <int DT, bool WIDE>
@@ -510,6 +546,14 @@ struct SparseCellEmit
     }
 };
 
+// Blocks of the two point passes: up to 8 per SM.
+int dense_grid(const McPlan& p)
+{
+    const int64_t tiles = (p.points + kScanTile - 1) / kScanTile;
+    const int64_t cap = 8LL * sm_count();
+    return static_cast<int>(tiles < cap ? tiles : cap);
+}
+
 template <int DT, bool WIDE>
 void dense_count(const McPlan& p, cudaStream_t s)
 {
@@ -520,8 +564,8 @@ void dense_count(const McPlan& p, cudaStream_t s)
         run_scan(GroupCount{ p.groups }, GroupEmit{ p.groups }, VertTotal{ p.ctr }, Count{ nullptr, p.ngroups },
                  p.ngroups, p.tiles_verts, &p.ctr->scan_verts, s);
     }
-    run_scan_reduce(DenseCellCount<DT, WIDE>{ p }, SoupTotal{ p.ctr }, Count{ nullptr, p.points }, p.points,
-                    p.tiles_soup, &p.ctr->scan_soup, s);
+    mc_dense_codes_kernel<DT, WIDE><<<dense_grid(p), kScanThreads, 0, s>>>(p);
+    TH_LAUNCH_CHECK();
 }
 
 template <int DT, bool WIDE>
@@ -532,8 +576,8 @@ void dense_emit(const McPlan& p, float* verts, int64_t* faces, cudaStream_t s)
         mc_dense_verts_kernel<DT, WIDE><<<grid_for(p.ngroups * 32, 256), 256, 0, s>>>(p, verts);
         TH_LAUNCH_CHECK();
     }
-    run_scan_apply(DenseCellCount<DT, WIDE>{ p }, DenseCellEmit<DT, WIDE>{ p, verts, faces },
-                   Count{ nullptr, p.points }, p.points, p.tiles_soup, s);
+    mc_dense_emit_kernel<DT, WIDE><<<dense_grid(p), kScanThreads, 0, s>>>(p, verts, faces);
+    TH_LAUNCH_CHECK();
 }
 
 template <int DT>

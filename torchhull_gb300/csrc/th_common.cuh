@@ -289,29 +289,15 @@ struct NoEpilogue
     __device__ void operator()(unsigned long long) const {}
 };
 
-// epi(total) runs once, on one thread, after all tile offsets are final.
-template <class CountF, class EpiF>
-__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(CountF count,
-                                                                   Count n_src,
-                                                                   unsigned long long* __restrict__ tile_sums,
-                                                                   ScanState* __restrict__ state,
-                                                                   EpiF epi)
+// Called by every block of a tile-sum kernel after its last tile sum is
+// written: the block that finishes last turns tile_sums[0, ntiles) into
+// exclusive offsets (no inter-block waiting) and runs epi(total) once.
+template <class EpiF>
+__device__ __forceinline__ void finish_tile_sums(int64_t ntiles,
+                                                 unsigned long long* __restrict__ tile_sums,
+                                                 ScanState* __restrict__ state,
+                                                 EpiF epi)
 {
-    const int64_t n = n_src.get();
-    const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
-    {
-        unsigned long long s = 0;
-        const int64_t base = tile * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
-#pragma unroll
-        for (int k = 0; k < kScanItems; ++k)
-            if (base + k < n)
-                s += count(base + k);
-        unsigned long long tot;
-        block_exclusive_scan(s, &tot);
-        if (threadIdx.x == 0)
-            tile_sums[tile] = tot;
-    }
     __threadfence();
     __shared__ bool is_last;
     if (threadIdx.x == 0)
@@ -338,6 +324,32 @@ __global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(CountF count,
         state->blocks_done = 0;
         epi(carry);
     }
+}
+
+// epi(total) runs once, on one thread, after all tile offsets are final.
+template <class CountF, class EpiF>
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(CountF count,
+                                                                   Count n_src,
+                                                                   unsigned long long* __restrict__ tile_sums,
+                                                                   ScanState* __restrict__ state,
+                                                                   EpiF epi)
+{
+    const int64_t n = n_src.get();
+    const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+    {
+        unsigned long long s = 0;
+        const int64_t base = tile * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            if (base + k < n)
+                s += count(base + k);
+        unsigned long long tot;
+        block_exclusive_scan(s, &tot);
+        if (threadIdx.x == 0)
+            tile_sums[tile] = tot;
+    }
+    finish_tile_sums(ntiles, tile_sums, state, epi);
 }
 
 // emit(i, exclusive_offset, count) is called for every item (count may be 0).

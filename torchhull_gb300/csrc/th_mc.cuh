@@ -52,7 +52,7 @@ struct McPlan
     unsigned long long* keys; // sparse: open-addressing table of ravel ids
     int32_t* slots;           // sparse: entry index of each key
     uint64_t hmask;           // table capacity - 1 (a power of two minus one)
-    uint8_t* codes;           // sparse: cell code of each entry (0: no cell)
+    uint8_t* codes;           // cell code of each point (dense) or entry (sparse); 0: no cell
     uint32_t* used;           // sparse, unique: vertex edge bits of each entry
     unsigned long long* vbase; // sparse, unique: first vertex of each entry
     unsigned long long* tiles_soup;
