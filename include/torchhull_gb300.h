@@ -212,6 +212,37 @@ th_status th_marching_cubes(th_context* ctx, const th_mc_args* args, void* strea
 th_status th_marching_cubes_export(th_context* ctx, float* verts, int64_t* faces, void* stream);
 
 /*
+ * Wireframe of one candidate level: torchhull::candidate_voxels_to_wireframes
+ * (visual_hull.h, visual_hull.cpp:141-155; visual_hull_cuda.cu:1024-1111),
+ * called once per entry of the candidate list.  candidates: [n] int64 device
+ * ids ravelled at resolution 2^level_index (x fastest); verts: [8n,3] float32
+ * and edges: [12n,2] int64 device buffers of the caller.
+ */
+th_status th_candidate_wireframe(th_context* ctx,
+                                 const int64_t* candidates,
+                                 int64_t n,
+                                 int32_t level_index,
+                                 const float cube_corner_bfl[3],
+                                 float cube_length,
+                                 float* verts,
+                                 int64_t* edges,
+                                 void* stream);
+
+/*
+ * torchhull::store_curve_network (io.h; io.cpp:11-127): writes a curve network
+ * (host arrays verts [nv,3] float32, edges [ne,2] int64) as ".obj" text or
+ * ".ply" binary little endian, chosen by the file extension.  Host only (no
+ * device needed); ctx may be NULL, else it receives the error message.
+ */
+th_status th_store_curve_network(th_context* ctx,
+                                 const char* filename,
+                                 const float* verts,
+                                 int64_t nv,
+                                 const int64_t* edges,
+                                 int64_t ne,
+                                 int32_t verbose);
+
+/*
  * Batched form: n independent requests processed together (shared launches,
  * one device->host read for all).  infos[n] receives the sizes; results stay
  * in the context until the next batched call.  No counterpart in the

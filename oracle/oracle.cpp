@@ -1276,3 +1276,37 @@ void oracle_mesh_free(oracle_mesh* m)
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// candidate_voxels_to_wireframes (visual_hull_cuda.cu:1024-1111), one level
+
+extern "C" void oracle_candidate_wireframe(const int64_t* candidates,
+                                           int64_t n,
+                                           int level_index,
+                                           float corner_x,
+                                           float corner_y,
+                                           float corner_z,
+                                           float cube_length,
+                                           float* verts,
+                                           int64_t* edges)
+{
+    // edge_to_vertex_table (marching_cubes_table.h:335-338)
+    static const int e2v[12][2] = { { 0, 1 }, { 1, 5 }, { 4, 5 }, { 0, 4 }, { 2, 3 }, { 3, 7 },
+                                    { 6, 7 }, { 2, 6 }, { 0, 2 }, { 1, 3 }, { 5, 7 }, { 4, 6 } };
+    const int64_t r = int64_t{ 1 } << level_index;
+    const float step = cube_length / static_cast<float>(r);
+    const float c[3] = { corner_x, corner_y, corner_z };
+    for (int64_t t = 0; t < n; ++t)
+    {
+        const int64_t id = candidates[t];
+        const int64_t g[3] = { id % r, (id / r) % r, id / (r * r) };
+        for (int i = 0; i < 8; ++i)
+            for (int a = 0; a < 3; ++a)
+                verts[3 * (8 * t + i) + a] = std::fma(step, static_cast<float>(g[a] + ((i >> a) & 1)), c[a]);
+        for (int i = 0; i < 12; ++i)
+        {
+            edges[2 * (12 * t + i) + 0] = 8 * t + e2v[i][0];
+            edges[2 * (12 * t + i) + 1] = 8 * t + e2v[i][1];
+        }
+    }
+}

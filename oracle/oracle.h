@@ -118,6 +118,18 @@ int64_t oracle_mesh_num_faces(const oracle_mesh* m);
 void oracle_mesh_copy(const oracle_mesh* m, float* verts, int64_t* faces);
 void oracle_mesh_free(oracle_mesh* m);
 
+// candidate_voxels_to_wireframes for one candidate level (ids ravelled at
+// resolution 2^level_index): verts [8n,3], edges [12n,2].
+void oracle_candidate_wireframe(const int64_t* candidates,
+                                int64_t n,
+                                int level_index,
+                                float corner_x,
+                                float corner_y,
+                                float corner_z,
+                                float cube_length,
+                                float* verts,
+                                int64_t* edges);
+
 #ifdef __cplusplus
 }
 #endif

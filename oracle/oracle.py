@@ -70,6 +70,7 @@ def lib() -> ctypes.CDLL:
             getattr(L, name).argtypes = [vp]
         L.oracle_mesh_copy.argtypes = [vp, vp, vp]
         L.oracle_mesh_free.argtypes = [vp]
+        L.oracle_candidate_wireframe.argtypes = [vp, i64, i32, f32, f32, f32, f32, vp, vp]
         _lib = L
     return _lib
 
@@ -175,6 +176,20 @@ def marching_cubes(volume=None, isolevel=0.0, return_local_coords=True, unique_v
     finally:
         L.oracle_mesh_free(h)
     return verts, faces
+
+
+def candidate_voxels_to_wireframes(candidate_voxels, cube_corner_bfl, cube_length):
+    out = []
+    for i, c in enumerate(candidate_voxels):
+        ids = np.ascontiguousarray(_as_array(c), dtype=np.int64)
+        n = ids.size
+        verts = np.empty((8 * n, 3), dtype=np.float32)
+        edges = np.empty((12 * n, 2), dtype=np.int64)
+        lib().oracle_candidate_wireframe(ids.ctypes.data, n, i, float(cube_corner_bfl[0]), float(cube_corner_bfl[1]),
+                                         float(cube_corner_bfl[2]), float(cube_length), verts.ctypes.data,
+                                         edges.ctypes.data)
+        out.append((verts, edges))
+    return out
 
 
 def nthreads_default() -> int:

@@ -1,8 +1,9 @@
 """GB300 (sm_103a) implementation of torchhull's visual-hull and blur path.
 
 Drop-in for ``torchhull.visual_hull``, ``torchhull.visual_hull_with_candidate_voxels``,
-``torchhull.sparse_visual_hull_field``, ``torchhull.marching_cubes`` and
-``torchhull.gaussian_blur``: same
+``torchhull.sparse_visual_hull_field``, ``torchhull.marching_cubes``,
+``torchhull.candidate_voxels_to_wireframes``, ``torchhull.store_curve_network``
+and ``torchhull.gaussian_blur`` (the reference's whole public API): same
 argument names, defaults, outputs and errors.  The work runs in hand-written
 CUDA behind the C ABI of ``include/torchhull_gb300.h``; there is no CPU path,
 and CPU tensors raise the reference's "No backend implementation" error.
@@ -22,10 +23,12 @@ import torch
 from . import build as _build
 
 __all__ = [
+    "candidate_voxels_to_wireframes",
     "gaussian_blur",
     "integral_image",
     "marching_cubes",
     "sparse_visual_hull_field",
+    "store_curve_network",
     "visual_hull",
     "visual_hull_with_candidate_voxels",
 ]
@@ -52,6 +55,8 @@ visual_hull_with_candidate_voxels = _C.visual_hull_with_candidate_voxels
 gaussian_blur = _C.gaussian_blur
 integral_image = _C.integral_image
 marching_cubes = _C.marching_cubes
+candidate_voxels_to_wireframes = _C.candidate_voxels_to_wireframes
+store_curve_network = _C.store_curve_network
 
 
 def sparse_visual_hull_field(

@@ -1265,6 +1265,53 @@ th_status th_marching_cubes_export(th_context* ctx, float* verts, int64_t* faces
     });
 }
 
+th_status th_candidate_wireframe(th_context* ctx,
+                                 const int64_t* candidates,
+                                 int64_t n,
+                                 int32_t level_index,
+                                 const float cube_corner_bfl[3],
+                                 float cube_length,
+                                 float* verts,
+                                 int64_t* edges,
+                                 void* stream)
+{
+    return guarded(ctx, [&] {
+        if (n < 0 || level_index < 0 || level_index > 20 || !cube_corner_bfl)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "invalid wireframe arguments" };
+        if (n > 0 && (!candidates || !verts || !edges))
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "candidates, verts or edges pointer is NULL" };
+        launch_wireframe(candidates, n, level_index, cube_corner_bfl, cube_length, verts, edges,
+                         static_cast<cudaStream_t>(stream));
+    });
+}
+
+th_status th_store_curve_network(th_context* ctx,
+                                 const char* filename,
+                                 const float* verts,
+                                 int64_t nv,
+                                 const int64_t* edges,
+                                 int64_t ne,
+                                 int32_t verbose)
+{
+    // host only: no device is needed, ctx (may be NULL) only receives the message
+    if (ctx)
+        ctx->error.clear();
+    if (!filename || nv < 0 || ne < 0 || (nv > 0 && !verts) || (ne > 0 && !edges))
+        return fail(ctx, TH_ERR_INVALID_ARGUMENT, "invalid curve network arguments");
+    const std::string name(filename);
+    try
+    {
+        if (!store_curve_network(name, verts, nv, edges, ne, verbose != 0))
+            return fail(ctx, TH_ERR_INVALID_ARGUMENT,
+                        "No implementation for file extension \"" + file_extension(name) + "\".");
+    }
+    catch (const std::exception& e)
+    {
+        return fail(ctx, TH_ERR_INVALID_ARGUMENT, e.what());
+    }
+    return TH_OK;
+}
+
 th_status th_visual_hull_batch(th_context* ctx, const th_hull_args* args, int32_t n, void* stream, th_hull_info* infos)
 {
     return guarded(ctx, [&] {

@@ -75,4 +75,10 @@ void launch_gaussian_blur(const void* images,
                           uint8_t* edge_tiles,
                           cudaStream_t s);
 
+// Candidate wireframe of one level (wire.cu): verts [8n,3], edges [12n,2].
+void launch_wireframe(const int64_t* cand, int64_t n, int shift, const float corner[3], float length, float* verts, int64_t* edges, cudaStream_t s);
+// OBJ/PLY writer (wire.cu); false for an unsupported extension.
+std::string file_extension(const std::string& filename);
+bool store_curve_network(const std::string& filename, const float* verts, int64_t nv, const int64_t* edges, int64_t ne, bool verbose);
+
 } // namespace th

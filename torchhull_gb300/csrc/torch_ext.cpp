@@ -332,6 +332,60 @@ std::tuple<at::Tensor, at::Tensor> marching_cubes(const at::Tensor& volume,
     return { verts, faces };
 }
 
+// torchhull::candidate_voxels_to_wireframes (visual_hull.cpp:141-155,
+// visual_hull_cuda.cu:1060-1111): per candidate level, 8 corners and 12
+// edges per voxel.
+std::vector<std::tuple<at::Tensor, at::Tensor>> candidate_voxels_to_wireframes(
+        const std::vector<at::Tensor>& candidate_voxels,
+        const std::array<float, 3>& cube_corner_bfl,
+        float cube_length)
+{
+    TH_CHECK_EQ(candidate_voxels.empty(), false);
+    require_cuda(candidate_voxels[0]);
+    for (const auto& c : candidate_voxels)
+        TH_CHECK_EQ(c.device(), candidate_voxels[0].device());
+    at::cuda::CUDAGuard guard(candidate_voxels[0].device());
+    const auto dev = candidate_voxels[0].device();
+    DeviceContext& dc = context_for(dev.index());
+    std::lock_guard<std::mutex> g(dc.lock);
+    void* stream = stream_of(candidate_voxels[0]);
+    std::vector<std::tuple<at::Tensor, at::Tensor>> out;
+    for (size_t i = 0; i < candidate_voxels.size(); ++i)
+    {
+        const at::Tensor c = candidate_voxels[i].contiguous();
+        TORCH_CHECK(c.scalar_type() == at::kLong, "expected scalar type Long but found ", c.scalar_type());
+        const int64_t n = c.numel();
+        at::Tensor verts = at::empty({ 8 * n, 3 }, at::TensorOptions().dtype(at::kFloat).device(dev));
+        at::Tensor edges = at::empty({ 12 * n, 2 }, at::TensorOptions().dtype(at::kLong).device(dev));
+        check(th_candidate_wireframe(dc.ctx, c.data_ptr<int64_t>(), n, static_cast<int32_t>(i), cube_corner_bfl.data(),
+                                     cube_length, verts.data_ptr<float>(), edges.data_ptr<int64_t>(), stream),
+              dc.ctx);
+        out.emplace_back(verts, edges);
+    }
+    return out;
+}
+
+// torchhull::store_curve_network (io.cpp:116-127).
+void store_curve_network(const std::string& filename,
+                         const std::tuple<at::Tensor, at::Tensor>& curve_network,
+                         bool verbose)
+{
+    const at::Tensor verts = std::get<0>(curve_network).to(at::kCPU).to(at::kFloat).contiguous();
+    const at::Tensor edges = std::get<1>(curve_network).to(at::kCPU).to(at::kLong).contiguous();
+    TORCH_CHECK(verts.dim() == 2 && verts.size(1) == 3, "curve network vertices must be |V| x 3");
+    TORCH_CHECK(edges.dim() == 2 && edges.size(1) == 2, "curve network edges must be |E| x 2");
+    const th_status st = th_store_curve_network(nullptr, filename.c_str(), verts.data_ptr<float>(), verts.size(0),
+                                                edges.data_ptr<int64_t>(), edges.size(0), verbose ? 1 : 0);
+    if (st != TH_OK)
+    {
+        const size_t dot = filename.find_last_of('.');
+        const size_t slash = filename.find_last_of('/');
+        const size_t name = slash == std::string::npos ? 0 : slash + 1;
+        const std::string ext = (dot == std::string::npos || dot <= name) ? std::string() : filename.substr(dot);
+        TORCH_CHECK(false, "No implementation for file extension \"" + ext + "\".");
+    }
+}
+
 at::Tensor integral_image(const at::Tensor& masks_in)
 {
     require_cuda(masks_in);
@@ -534,6 +588,11 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
           "unique_verts"_a = true,
           "Marching Cubes on a 1 x D x H x W dense or sparse COO volume; returns (verts [V,3] float32, "
           "faces [F,3] int64).");
+    m.def("candidate_voxels_to_wireframes", &candidate_voxels_to_wireframes, "candidate_voxels"_a,
+          "cube_corner_bfl"_a, "cube_length"_a,
+          "Wireframes (verts [8N,3] float32, edges [12N,2] int64) of each candidate level.");
+    m.def("store_curve_network", &store_curve_network, "filename"_a, "curve_network"_a, "verbose"_a = false,
+          "Stores a curve network (verts, edges) as .obj or .ply.");
     m.def("integral_image", &integral_image, "masks"_a, "Float32 integral image [B,H,W] of masks [B,H,W,1].");
     m.def("device_pool_bytes", &device_pool_bytes, "device"_a, "Bytes held by the device's resident pools.");
     m.def("set_profiling", &set_profiling, "device"_a, "enable"_a, "Record CUDA events between hull stages.");
