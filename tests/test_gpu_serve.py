@@ -26,11 +26,14 @@ def alone(th, r):
     return v.cpu(), f.cpu()
 
 
-def test_results_in_the_mix_equal_results_alone(th, cuda, requests):
+@pytest.mark.parametrize("priority", ["large_first", "small_first", "none"])
+def test_results_in_the_mix_equal_results_alone(th, cuda, requests, priority):
     from torchhull_gb300.serve import HullServer
 
     expected = [alone(th, r) for r in requests]
-    with HullServer(device=cuda.index or 0, slots=3, budget_bytes=20e9) as server:
+    # large_bytes splits the mix so both stream priorities carry requests
+    with HullServer(device=cuda.index or 0, slots=3, budget_bytes=20e9, priority=priority,
+                    large_bytes=2e8) as server:
         futures = [server.submit(r) for r in requests + requests]
         got = [f.result(timeout=120) for f in futures]
         stats = server.stats()
@@ -59,3 +62,10 @@ def test_request_larger_than_budget_is_refused(cuda, requests):
     with HullServer(device=cuda.index or 0, slots=1, budget_bytes=1e6) as server:
         with pytest.raises(ValueError):
             server.submit(requests[0])
+
+
+def test_unknown_priority_policy_is_refused(cuda):
+    from torchhull_gb300.serve import HullServer
+
+    with pytest.raises(ValueError):
+        HullServer(device=cuda.index or 0, slots=1, priority="fastest")

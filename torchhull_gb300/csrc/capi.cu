@@ -937,6 +937,11 @@ void run_mc(McSlot& s, const th_mc_args* a, cudaStream_t st)
         p.volume = a->volume;
         p.points = D * H * W;
         p.wide = p.points >= (int64_t{ 1 } << 32);
+        if (!p.wide)
+        {
+            p.div_w = make_fastdiv(static_cast<uint32_t>(W));
+            p.div_h = make_fastdiv(static_cast<uint32_t>(H));
+        }
         p.ngroups = (p.points + 31) / 32;
     }
 

@@ -95,12 +95,12 @@ __device__ __forceinline__ void decode(const McPlan& p, int64_t q, int64_t& x, i
     }
     else
     {
-        const uint32_t qq = static_cast<uint32_t>(q), w = static_cast<uint32_t>(p.W), h = static_cast<uint32_t>(p.H);
-        const uint32_t r = qq / w;
-        x = qq - r * w;
-        const uint32_t zz = r / h;
+        const uint32_t qq = static_cast<uint32_t>(q);
+        const uint32_t r = fast_div(p.div_w, qq);
+        x = qq - r * p.div_w.d;
+        const uint32_t zz = fast_div(p.div_h, r);
         z = zz;
-        y = r - zz * h;
+        y = r - zz * p.div_h.d;
     }
 }
 
@@ -262,25 +262,45 @@ __global__ void __launch_bounds__(kScanThreads) mc_dense_codes_kernel(McPlan p)
     finish_tile_sums(ntiles, p.tiles_soup, &p.ctr->scan_soup, SoupTotal{ p.ctr });
 }
 
-// Pass 2: the same rounds, each one block scan of the counts, then the
-// active cells' soup.
+// Pass 2, over the same tiles with kScanItems consecutive points per thread
+// (one 8-byte read of codes, one block scan per tile): the active cells' soup.
 template <int DT, bool WIDE>
 __global__ void __launch_bounds__(kScanThreads) mc_dense_emit_kernel(McPlan p, float* __restrict__ verts, int64_t* __restrict__ faces)
 {
+    static_assert(kScanItems == 8, "one 8-byte read of codes per thread");
     const int64_t ntiles = (p.points + kScanTile - 1) / kScanTile;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
     {
-        unsigned long long off = p.tiles_soup[tile];
+        const int64_t base = tile * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
+        uint32_t lo = 0, hi = 0;
+        if (base + kScanItems <= p.points)
+        {
+            const uint2 w = *reinterpret_cast<const uint2*>(p.codes + base);
+            lo = w.x;
+            hi = w.y;
+        }
+        else
+        {
+            for (int k = 0; k < kScanItems && base + k < p.points; ++k)
+                (k < 4 ? lo : hi) |= static_cast<uint32_t>(p.codes[base + k]) << (8 * (k & 3));
+        }
+        unsigned long long s = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            s += mc_count[((k < 4 ? lo : hi) >> (8 * (k & 3))) & 0xffu];
+        unsigned long long tot;
+        unsigned long long off = block_exclusive_scan(s, &tot) + p.tiles_soup[tile];
+        if (s == 0)
+            continue;
         for (int k = 0; k < kScanItems; ++k)
         {
-            const int64_t q = tile * kScanTile + k * kScanThreads + threadIdx.x;
-            const int code = q < p.points ? p.codes[q] : 0;
+            const int code = static_cast<int>(((k < 4 ? lo : hi) >> (8 * (k & 3))) & 0xffu);
             const int cnt = mc_count[code];
-            unsigned long long tot;
-            const unsigned long long ex = block_exclusive_scan(static_cast<unsigned long long>(cnt), &tot);
             if (cnt)
-                dense_emit_cell<DT, WIDE>(p, q, code, off + ex, cnt, verts, faces);
-            off += tot;
+            {
+                dense_emit_cell<DT, WIDE>(p, base + k, code, off, cnt, verts, faces);
+                off += cnt;
+            }
         }
     }
 }

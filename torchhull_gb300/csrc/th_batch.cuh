@@ -30,6 +30,7 @@ struct BatchReq
 struct BatchCounters
 {
     int64_t count[kMaxLevel + 2];            // entries of level i (all requests)
+    unsigned long long head[kMaxLevel + 2];  // dequeue position of level i
     unsigned long long overflow;
 };
 

@@ -187,6 +187,35 @@ __device__ __forceinline__ bool round_small(float v, Snapped& out)
     return true;
 }
 
+// Unsigned 32-bit division by a run-time invariant divisor with one high
+// multiply (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", 1994, Fig. 4.1): l = ceil(log2 d),
+// m = floor(2^32 (2^l - d) / d) + 1, q = (t + ((n - t) >> min(l,1))) >> max(l-1,0)
+// with t = mulhi(m, n); exact for every 32-bit n and d >= 1.
+struct FastDiv
+{
+    uint32_t d, m, s1, s2;
+};
+
+inline FastDiv make_fastdiv(uint32_t d)
+{
+    uint32_t l = 0;
+    while (l < 32 && (uint64_t{ 1 } << l) < d)
+        ++l;
+    FastDiv f;
+    f.d = d;
+    f.m = static_cast<uint32_t>(((uint64_t{ 1 } << 32) * ((uint64_t{ 1 } << l) - d)) / d + 1);
+    f.s1 = l < 1 ? l : 1;
+    f.s2 = l > 1 ? l - 1 : 0;
+    return f;
+}
+
+__device__ __forceinline__ uint32_t fast_div(const FastDiv& f, uint32_t n)
+{
+    const uint32_t t = __umulhi(f.m, n);
+    return (t + ((n - t) >> f.s1)) >> f.s2;
+}
+
 // K*T*[x,y,z,1] with nested fmaf (visual_hull_cuda.cu:142-156). m is row-major 4x4.
 __device__ __forceinline__ float project_row(const float* m, float x, float y, float z)
 {

@@ -40,6 +40,7 @@ struct McPlan
     bool wide;             // points >= 2^32: 64-bit index decoding
     int64_t D, H, W;       // volume sizes along z, y, x
     int64_t points;        // D * H * W
+    FastDiv div_w, div_h;  // by W and by H (points < 2^32)
     float iso;
     float scale[3];        // 2 / (size - 1) along x, y, z
     const void* volume;    // dense: [D, H, W], x fastest

@@ -67,9 +67,17 @@ class _Job:
 class HullServer:
     """Continuous-batching visual-hull server on one device."""
 
-    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: float = 60e9):
+    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: float = 60e9, priority: str = "large_first",
+                 large_bytes: float = 2e9):
+        """priority: which requests run on high-priority CUDA streams, so that the block scheduler
+        prefers their kernels while others are running: "large_first" (requests whose estimated
+        device memory exceeds large_bytes; they set the tail latency), "small_first", or "none"."""
+        if priority not in ("large_first", "small_first", "none"):
+            raise ValueError(f"unknown priority policy {priority!r}")
         self.device = torch.device("cuda", device)
         self.budget = int(budget_bytes)
+        self.priority = priority
+        self.large_bytes = int(large_bytes)
         self._cv = threading.Condition()
         self._pending: collections.deque[_Job] = collections.deque()
         self._in_flight = 0
@@ -80,6 +88,7 @@ class HullServer:
         self.completed = 0
         self._contexts = [_C.HullContext(device) for _ in range(slots)]
         self._streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        self._streams_hi = [torch.cuda.Stream(self.device, priority=-1) for _ in range(slots)]
         self._threads = [threading.Thread(target=self._worker, args=(i,), daemon=True) for i in range(slots)]
         for t in self._threads:
             t.start()
@@ -132,8 +141,13 @@ class HullServer:
                 return job
         return None
 
+    def _stream_for(self, slot: int, job: _Job) -> torch.cuda.Stream:
+        large = job.bytes > self.large_bytes
+        hi = (self.priority == "large_first" and large) or (self.priority == "small_first" and not large)
+        return self._streams_hi[slot] if hi else self._streams[slot]
+
     def _worker(self, slot: int) -> None:
-        ctx, stream = self._contexts[slot], self._streams[slot]
+        ctx = self._contexts[slot]
         while True:
             with self._cv:
                 job = None
@@ -146,6 +160,7 @@ class HullServer:
                 self._in_flight += 1
                 self._running_bytes += job.bytes
             job.started = time.perf_counter()
+            stream = self._stream_for(slot, job)
             try:
                 r = job.req
                 with torch.cuda.stream(stream):
