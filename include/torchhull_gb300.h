@@ -104,6 +104,22 @@ typedef struct th_hull_info
  */
 th_status th_visual_hull(th_context* ctx, const th_hull_args* args, void* stream, th_hull_info* info);
 
+/*
+ * Fused blur -> hull request: the visual hull of gaussian_blur(masks,
+ * kernel_size, sigma, sparse=True) (blurred in the masks' own float type),
+ * with the blurred masks kept in a context pool instead of a tensor the caller
+ * allocates and passes back.  Results (and the export calls) are identical to
+ * th_gaussian_blur followed by th_visual_hull on its output.  No reference
+ * counterpart as one call; it chains gaussian_blur.cpp:15-28 and
+ * visual_hull.cpp:34-83.
+ */
+th_status th_visual_hull_blurred(th_context* ctx,
+                                 const th_hull_args* args,
+                                 int32_t kernel_size,
+                                 float sigma,
+                                 void* stream,
+                                 th_hull_info* info);
+
 /* Writes the mesh of the last th_visual_hull call: verts [V,3] float32 in world
  * coordinates, faces [F,3] int64 with torchhull's winding (columns 1 and 2
  * swapped, visual_hull_cuda.cu:941-956).  Either pointer may be NULL when its

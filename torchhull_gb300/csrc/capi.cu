@@ -307,6 +307,7 @@ struct th_context
     std::vector<th::HullSlot> batch;
     th::BatchState bstate;
     th::DevBuf blur_scratch;
+    th::DevBuf blurred; // masks blurred by th_visual_hull_blurred
     th::McSlot mc;
     bool profiling = false;
     th::StageEvents events;
@@ -329,7 +330,8 @@ int64_t pool_bytes(const th_context* ctx)
             b += static_cast<int64_t>(d->bytes);
         return b;
     };
-    int64_t total = sum(ctx->hull) + static_cast<int64_t>(ctx->blur_scratch.bytes);
+    int64_t total = sum(ctx->hull) + static_cast<int64_t>(ctx->blur_scratch.bytes) +
+                    static_cast<int64_t>(ctx->blurred.bytes);
     for (const DevBuf* d : ctx->mc.buffers())
         total += static_cast<int64_t>(d->bytes);
     for (const auto& s : ctx->batch)
@@ -876,6 +878,34 @@ namespace th
 namespace
 {
 
+// gaussian_blur_cuda.cu:294-305 and :79-81, in the reference's order.
+void check_blur_args(int32_t images_dtype, int32_t kernel_size, float sigma, int32_t out_dtype)
+{
+    if (kernel_size <= 0)
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT,
+                        "Check failed: kernel_size > 0 (" + std::to_string(kernel_size) + " vs. 0)" };
+    if (kernel_size % 2 != 1)
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT,
+                        "Check failed: kernel_size % 2 == 1 (" + std::to_string(kernel_size % 2) + " vs. 1)" };
+    if (!(sigma > 0.f))
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: sigma > 0.f" };
+    if (!(out_dtype == TH_FLOAT16 || out_dtype == TH_FLOAT32 || out_dtype == TH_FLOAT64))
+    {
+        if (out_dtype == TH_BFLOAT16)
+            throw ArgError{ TH_ERR_UNSUPPORTED_DTYPE, "\"tile_convolution_kernel\" not implemented for 'BFloat16'" };
+        throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: torch::isFloatingType(dtype_result) == true" };
+    }
+    if (!is_image_dtype(images_dtype))
+        throw ArgError{ TH_ERR_UNSUPPORTED_DTYPE,
+                        std::string("\"edge_kernel\" not implemented for '") + dtype_name(images_dtype) + "'" };
+}
+
+// Element size of a float dtype code.
+size_t float_size(int32_t dt)
+{
+    return dt == TH_FLOAT64 ? 8 : (dt == TH_FLOAT32 ? 4 : 2);
+}
+
 std::string float_text(float v)
 {
     std::ostringstream os;
@@ -1039,6 +1069,7 @@ void th_context_destroy(th_context* ctx)
     for (auto& s : ctx->batch)
         s.release();
     ctx->blur_scratch.release();
+    ctx->blurred.release();
     ctx->mc.release();
     ctx->bstate.release();
     ctx->events.destroy();
@@ -1121,6 +1152,38 @@ th_status th_visual_hull(th_context* ctx, const th_hull_args* args, void* stream
     });
 }
 
+th_status th_visual_hull_blurred(th_context* ctx,
+                                 const th_hull_args* args,
+                                 int32_t kernel_size,
+                                 float sigma,
+                                 void* stream,
+                                 th_hull_info* info)
+{
+    return guarded(ctx, [&] {
+        if (!args)
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "args is NULL" };
+        // gaussian_blur(masks, kernel_size, sigma) first: its checks come first
+        check_blur_args(args->masks_dtype, kernel_size, sigma, args->masks_dtype);
+        validate(args);
+        auto st = static_cast<cudaStream_t>(stream);
+        th_hull_args a = *args;
+        const int64_t n = args->batch * args->height * args->width;
+        if (n > 0)
+        {
+            ctx->blurred.ensure(float_size(args->masks_dtype) * static_cast<size_t>(n));
+            const int64_t bytes = blur_tile_bytes(args->batch, args->height, args->width, kernel_size);
+            if (bytes > 0)
+                ctx->blur_scratch.ensure(static_cast<size_t>(bytes));
+            launch_gaussian_blur(args->masks, args->masks_dtype, args->batch, args->height, args->width, kernel_size,
+                                 sigma, true, ctx->blurred.p, args->masks_dtype, ctx->blur_scratch.as<uint8_t>(), st);
+            a.masks = ctx->blurred.p;
+        }
+        run_hull(ctx, ctx->hull, &a, st, ctx->profiling ? &ctx->events : nullptr);
+        if (info)
+            *info = ctx->hull.info;
+    });
+}
+
 th_status th_visual_hull_export(th_context* ctx, float* verts, int64_t* faces, void* stream)
 {
     return guarded(ctx, [&] {
@@ -1190,24 +1253,7 @@ th_status th_gaussian_blur(th_context* ctx,
                            void* stream)
 {
     return guarded(ctx, [&] {
-        // gaussian_blur_cuda.cu:294-305 and :79-81
-        if (kernel_size <= 0)
-            throw ArgError{ TH_ERR_INVALID_ARGUMENT,
-                            "Check failed: kernel_size > 0 (" + std::to_string(kernel_size) + " vs. 0)" };
-        if (kernel_size % 2 != 1)
-            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: kernel_size % 2 == 1 (" +
-                                                             std::to_string(kernel_size % 2) + " vs. 1)" };
-        if (!(sigma > 0.f))
-            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: sigma > 0.f" };
-        if (!(out_dtype == TH_FLOAT16 || out_dtype == TH_FLOAT32 || out_dtype == TH_FLOAT64))
-        {
-            if (out_dtype == TH_BFLOAT16)
-                throw ArgError{ TH_ERR_UNSUPPORTED_DTYPE, "\"tile_convolution_kernel\" not implemented for 'BFloat16'" };
-            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "Check failed: torch::isFloatingType(dtype_result) == true" };
-        }
-        if (!is_image_dtype(images_dtype))
-            throw ArgError{ TH_ERR_UNSUPPORTED_DTYPE,
-                            std::string("\"edge_kernel\" not implemented for '") + dtype_name(images_dtype) + "'" };
+        check_blur_args(images_dtype, kernel_size, sigma, out_dtype);
         if (batch < 0 || height < 0 || width < 0)
             throw ArgError{ TH_ERR_INVALID_ARGUMENT, "image sizes must be non-negative" };
         const int64_t n = batch * height * width;

@@ -167,7 +167,9 @@ HullOutputs run_visual_hull(const at::Tensor& masks_in,
                             const std::string& transforms_convention,
                             bool unique_verts,
                             bool want_candidates,
-                            bool want_field)
+                            bool want_field,
+                            int blur_kernel_size = 0,
+                            float blur_sigma = 0.f)
 {
     require_cuda(masks_in);
     at::cuda::CUDAGuard guard(masks_in.device());
@@ -180,7 +182,10 @@ HullOutputs run_visual_hull(const at::Tensor& masks_in,
     std::lock_guard<std::mutex> g(dc.lock);
     void* stream = stream_of(masks);
     th_hull_info info{};
-    check(th_visual_hull(dc.ctx, &a, stream, &info), dc.ctx);
+    if (blur_kernel_size != 0)
+        check(th_visual_hull_blurred(dc.ctx, &a, blur_kernel_size, blur_sigma, stream, &info), dc.ctx);
+    else
+        check(th_visual_hull(dc.ctx, &a, stream, &info), dc.ctx);
 
     const auto dev = masks.device();
     HullOutputs out;
@@ -218,6 +223,26 @@ std::tuple<at::Tensor, at::Tensor> visual_hull(const at::Tensor& masks,
 {
     auto o = run_visual_hull(masks, transforms, level, cube_corner_bfl, cube_length, masks_partial,
                              transforms_convention, unique_verts, false, false);
+    return { o.verts, o.faces };
+}
+
+// Fused blur -> hull: visual_hull(gaussian_blur(masks, kernel_size, sigma), ...)
+// with the blurred masks kept inside the library (no reference counterpart as
+// one call).
+std::tuple<at::Tensor, at::Tensor> visual_hull_blurred(const at::Tensor& masks,
+                                                       const at::Tensor& transforms,
+                                                       int level,
+                                                       const std::array<float, 3>& cube_corner_bfl,
+                                                       float cube_length,
+                                                       bool masks_partial,
+                                                       const std::string& transforms_convention,
+                                                       int kernel_size,
+                                                       float sigma,
+                                                       bool unique_verts)
+{
+    TORCH_CHECK(kernel_size != 0, "Check failed: kernel_size > 0 (0 vs. 0)");
+    auto o = run_visual_hull(masks, transforms, level, cube_corner_bfl, cube_length, masks_partial,
+                             transforms_convention, unique_verts, false, false, kernel_size, sigma);
     return { o.verts, o.faces };
 }
 
@@ -584,6 +609,11 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
           "Sparse hull field as (ravelled indices, values, grid size).");
     m.def("gaussian_blur", &gaussian_blur, "images"_a, "kernel_size"_a, "sigma"_a, "sparse"_a = true,
           "dtype"_a = pybind11::none(), "Gaussian blur of [B,H,W,1] images.");
+    m.def("visual_hull_blurred", &visual_hull_blurred, "masks"_a, "transforms"_a, "level"_a, "cube_corner_bfl"_a,
+          "cube_length"_a, "masks_partial"_a, "transforms_convention"_a, "kernel_size"_a, "sigma"_a,
+          "unique_verts"_a = true,
+          "visual_hull(gaussian_blur(masks, kernel_size, sigma), ...) in one request; the blurred masks stay in the "
+          "library.");
     m.def("marching_cubes", &marching_cubes, "volume"_a, "isolevel"_a, "return_local_coords"_a = true,
           "unique_verts"_a = true,
           "Marching Cubes on a 1 x D x H x W dense or sparse COO volume; returns (verts [V,3] float32, "
