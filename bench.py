@@ -23,6 +23,8 @@ requests (weak scaling, no collective on the data path).
 
 --mode hetero: 64 heterogeneous requests (views U{4..48}, side
 U{256,512,768,1024}, level U{6..9}, partial ~ Bernoulli(0.3)), batched vs plain.
+--mode blur: the blur configuration (24 OpenCV views of 512^2, blur k=9 sigma=2,
+level 8) as one fused request against blur and hull as two calls.
 --mode mc: torchhull.marching_cubes on the reference benchmark's sphere SDF
 volumes (100^3 .. 600^3, dense and sparse), ms per call.
 --mode serve: Poisson arrivals (default 200/s for 10 s) from a pool of
@@ -238,6 +240,8 @@ def run_gb300(args) -> dict | None:
         return finish(run_serve(args, th, scenes, dev, world, rank), world)
     if args.mode == "mc":
         return finish(run_mc(args, th, dev, world, rank), world)
+    if args.mode == "blur":
+        return finish(run_blur(args, th, scenes, dev, world, rank), world)
 
     Q = args.requests
     reqs = [scenes.partial_request(device=dev, seed=3 + 1000 * rank + q) for q in range(Q)]
@@ -447,6 +451,43 @@ def run_mc(args, th, dev, world, rank):
             "table": rows}
 
 
+def run_blur(args, th, scenes, dev, world, rank):
+    """The blur configuration: 5 ellipsoids, 24 OpenCV views of 512^2, blur k=9 sigma=2, then level 8."""
+    import torch
+
+    r = scenes.blur_request(device=dev, seed=2 + 1000 * rank)
+    hull_args = (r.transforms, r.level, r.cube_corner_bfl, r.cube_length, r.masks_partial, r.transforms_convention)
+
+    def two_calls():
+        return th.visual_hull(th.gaussian_blur(r.masks, 9, 2.0), *hull_args)
+
+    def fused():
+        return th.visual_hull_blurred(r.masks, *hull_args, 9, 2.0)
+
+    out = {}
+    for name, fn in (("fused", fused), ("two_calls", two_calls)):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        e1.synchronize()
+        out[name] = max_over_ranks(e0.elapsed_time(e1), world, dev) / args.steps
+    if rank != 0:
+        return None
+    return {"metric": "hulls/s, blur k=9 sigma=2 then level-8 hull, 24x512^2 OpenCV views (fused request)",
+            "value": 1000.0 * world / out["fused"], "unit": "hulls/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": out["fused"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded ray-ellipsoid masks",
+            "config": {"workload": "5 ellipsoids, 24 OpenCV views of 512x512 float32, gaussian_blur(k=9, sigma=2, "
+                                   "sparse), visual_hull level 8, full masks"},
+            "two_calls_ms": out["two_calls"], "fused_over_two_calls": out["two_calls"] / out["fused"]}
+
+
 def run_serve(args, th, scenes, dev, world, rank):
     import numpy as np
     import torch
@@ -573,7 +614,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--mode", choices=["headline", "hetero", "serve", "mc"], default="headline")
+    ap.add_argument("--mode", choices=["headline", "hetero", "serve", "mc", "blur"], default="headline")
     ap.add_argument("--requests", type=int, default=4)
     ap.add_argument("--cpu-samples", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -595,7 +595,17 @@ void run_hull_once(th_context* ctx,
         if (ovf & kOverflowCorners)
             s.corner_cap *= 4;
         if (attempt == 7)
-            throw ArgError{ TH_ERR_OUT_OF_MEMORY, "visual hull pools could not be grown enough" };
+        {
+            const DevCounters& c = *s.host;
+            std::string counts;
+            for (int i = 0; i <= L; ++i)
+                counts += (i ? "," : "") + std::to_string(c.level_count[i]);
+            throw ArgError{ TH_ERR_OUT_OF_MEMORY,
+                            "visual hull pools could not be grown enough (overflow " + std::to_string(ovf) +
+                                    ", level counts " + counts + ", corners " + std::to_string(c.corners) + ", rows " +
+                                    std::to_string(c.rows) + ", node cap " + std::to_string(p.node_cap) +
+                                    ", corner cap " + std::to_string(p.corner_cap) + ")" };
+        }
     }
     fill_info(s, &s.info);
     s.has_result = true;
