@@ -275,7 +275,7 @@ namespace
 // Pools and the last result of the public marching cubes.
 struct McSlot
 {
-    DevBuf groups, keys, slots, codes, used, vbase, tiles_soup, tiles_verts, ctr;
+    DevBuf groups, keys, slots, codes, used, vbase, tiles_soup, tiles_verts, active, active_soup, ctr;
     McCounters* host = nullptr; // pinned copy of the counters
     McPlan plan{};
     th_mc_info info{};
@@ -283,7 +283,7 @@ struct McSlot
 
     std::vector<const DevBuf*> buffers() const
     {
-        return { &groups, &keys, &slots, &codes, &used, &vbase, &tiles_soup, &tiles_verts, &ctr };
+        return { &groups, &keys, &slots, &codes, &used, &vbase, &tiles_soup, &tiles_verts, &active, &active_soup, &ctr };
     }
 
     void release()
@@ -392,21 +392,22 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool batch_slo
     const int64_t B = a->batch, H = a->height, W = a->width;
     const int64_t R = (int64_t{ 1 } << L) + 1;
     const int64_t WR = (R + 63) / 64;
-    if (s.node_cap == 0)
+    // Every request starts from at least the capacity its level could need up
+    // to 16 M nodes and corners (about 0.5 GB; a level-9 hull of 32 megapixel
+    // views fits without a rerun), whatever smaller requests the context
+    // served before; beyond that the pools grow x4 per rerun.  Batch slots
+    // keep no octree of their own and start at 4 M corners.
+    if (batch_slot)
     {
-        // 16 M nodes and corners (about 0.5 GB) cover a level-9 hull of 32
-        // megapixel views without a rerun; the pools grow x4 beyond that.
-        // Batch slots start at 4 M corners.
-        s.node_cap = batch_slot ? 1 : std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 24);
-        s.corner_cap = std::min<int64_t>(R * R * R, int64_t{ 1 } << (batch_slot ? 22 : 24));
-        s.parent_cap = batch_slot ? 1 : std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 22);
+        s.node_cap = std::max<int64_t>(s.node_cap, 1);
+        s.parent_cap = std::max<int64_t>(s.parent_cap, 1);
     }
-    if (!batch_slot)
+    else
     {
-        s.node_cap = std::max<int64_t>(s.node_cap, std::min<int64_t>(max_nodes(L), 4096));
-        s.parent_cap = std::max<int64_t>(s.parent_cap, std::min<int64_t>(max_nodes(L), 4096));
+        s.node_cap = std::max<int64_t>(s.node_cap, std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 24));
+        s.parent_cap = std::max<int64_t>(s.parent_cap, std::min<int64_t>(max_nodes(L), int64_t{ 1 } << 22));
     }
-    s.corner_cap = std::max<int64_t>(s.corner_cap, std::min<int64_t>(R * R * R, 4096));
+    s.corner_cap = std::max<int64_t>(s.corner_cap, std::min<int64_t>(R * R * R, int64_t{ 1 } << (batch_slot ? 22 : 24)));
     const int64_t node_cap = std::min<int64_t>(s.node_cap, max_nodes(L));
     const int64_t corner_cap = std::min<int64_t>(s.corner_cap, R * R * R);
     const int64_t parent_cap = std::min<int64_t>(s.parent_cap, node_cap);
@@ -1038,6 +1039,17 @@ void run_mc(McSlot& s, const th_mc_args* a, cudaStream_t st)
     if (c.flags & kMcUnsorted)
         throw ArgError{ TH_ERR_INVALID_ARGUMENT,
                         "sparse volume indices must be coalesced (strictly ascending in (z, y, x))" };
+    if (!p.sparse)
+    {
+        // packed (soup << 32 | active) tile sums: both totals below 2^32
+        if (c.active >= (1ull << 28))
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "marching cubes: more than 2^28 active cells" };
+        p.nactive = static_cast<int64_t>(c.active);
+        s.active.ensure(sizeof(int64_t) * std::max<int64_t>(p.nactive, 1));
+        s.active_soup.ensure(sizeof(unsigned long long) * std::max<int64_t>(p.nactive, 1));
+        p.active = s.active.as<int64_t>();
+        p.active_soup = s.active_soup.as<unsigned long long>();
+    }
     s.plan = p;
     s.info.num_faces = static_cast<int64_t>(c.soup / 3);
     s.info.num_verts = static_cast<int64_t>(p.unique ? c.verts : c.soup);

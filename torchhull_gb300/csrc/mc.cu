@@ -104,32 +104,44 @@ __device__ __forceinline__ void decode(const McPlan& p, int64_t q, int64_t& x, i
     }
 }
 
-// Edge bits of each group of 32 points (one warp per group).
+// Edge bits of each group of 32 points (one warp per group, four groups per
+// iteration so that their loads are in flight together).
 template <int DT, bool WIDE>
 __global__ void __launch_bounds__(256) mc_dense_edges_kernel(McPlan p)
 {
+    constexpr int kGroups = 4;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     const int64_t WH = p.W * p.H;
-    for (int64_t g = warp; g < p.ngroups; g += nwarps)
+    for (int64_t g0 = warp; g0 < p.ngroups; g0 += kGroups * nwarps)
     {
-        const int64_t q = g * 32 + lane;
-        bool ex = false, ey = false, ez = false;
-        if (q < p.points)
+        bool ex[kGroups], ey[kGroups], ez[kGroups];
+#pragma unroll
+        for (int j = 0; j < kGroups; ++j)
         {
-            int64_t x, y, z;
-            decode<WIDE>(p, q, x, y, z);
-            const bool b = below<DT>(p.volume, q, p.iso);
-            ex = x + 1 < p.W && below<DT>(p.volume, q + 1, p.iso) != b;
-            ey = y + 1 < p.H && below<DT>(p.volume, q + p.W, p.iso) != b;
-            ez = z + 1 < p.D && below<DT>(p.volume, q + WH, p.iso) != b;
+            const int64_t q = (g0 + j * nwarps) * 32 + lane;
+            ex[j] = ey[j] = ez[j] = false;
+            if (q < p.points)
+            {
+                int64_t x, y, z;
+                decode<WIDE>(p, q, x, y, z);
+                const bool b = below<DT>(p.volume, q, p.iso);
+                ex[j] = x + 1 < p.W && below<DT>(p.volume, q + 1, p.iso) != b;
+                ey[j] = y + 1 < p.H && below<DT>(p.volume, q + p.W, p.iso) != b;
+                ez[j] = z + 1 < p.D && below<DT>(p.volume, q + WH, p.iso) != b;
+            }
         }
-        const uint32_t X = __ballot_sync(0xffffffffu, ex);
-        const uint32_t Y = __ballot_sync(0xffffffffu, ey);
-        const uint32_t Z = __ballot_sync(0xffffffffu, ez);
-        if (lane == 0)
-            p.groups[g] = McGroup{ X, Y, Z, 0u, 0ull };
+#pragma unroll
+        for (int j = 0; j < kGroups; ++j)
+        {
+            const int64_t g = g0 + j * nwarps;
+            const uint32_t X = __ballot_sync(0xffffffffu, ex[j]);
+            const uint32_t Y = __ballot_sync(0xffffffffu, ey[j]);
+            const uint32_t Z = __ballot_sync(0xffffffffu, ez[j]);
+            if (lane == 0 && g < p.ngroups)
+                p.groups[g] = McGroup{ X, Y, Z, 0u, 0ull };
+        }
     }
 }
 
@@ -158,6 +170,17 @@ struct SoupTotal
     __device__ void operator()(unsigned long long t) const
     {
         ctr->soup = t;
+    }
+};
+
+// (soup << 32) | active cells of a dense volume
+struct PackedTotal
+{
+    McCounters* ctr;
+    __device__ void operator()(unsigned long long t) const
+    {
+        ctr->soup = t >> 32;
+        ctr->active = t & 0xffffffffull;
     }
 };
 
@@ -231,9 +254,10 @@ __device__ __forceinline__ void dense_emit_cell(const McPlan& p, int64_t q, int 
 }
 
 // Pass 1 over the points in tiles of kScanTile, each tile in kScanItems
-// rounds of kScanThreads consecutive points (coalesced corner loads): the
-// cell code of every point into codes[] (0 where no cell starts), the soup
-// vertex count of every tile into tiles_soup, then exclusive tile offsets.
+// rounds of kScanThreads consecutive points (coalesced corner loads, all
+// rounds in flight together): the cell code of every point into codes[] (0
+// where no cell starts) and, per tile, (soup vertices << 32) | active cells
+// into tiles_soup, then exclusive tile offsets of both.
 template <int DT, bool WIDE>
 __global__ void __launch_bounds__(kScanThreads) mc_dense_codes_kernel(McPlan p)
 {
@@ -241,7 +265,7 @@ __global__ void __launch_bounds__(kScanThreads) mc_dense_codes_kernel(McPlan p)
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
     {
         unsigned long long s = 0;
-#pragma unroll 2
+#pragma unroll
         for (int k = 0; k < kScanItems; ++k)
         {
             const int64_t q = tile * kScanTile + k * kScanThreads + threadIdx.x;
@@ -251,7 +275,8 @@ __global__ void __launch_bounds__(kScanThreads) mc_dense_codes_kernel(McPlan p)
                 const int c = dense_code<DT, WIDE>(p, q, x, y, z);
                 const int code = c < 0 ? 0 : c;
                 p.codes[q] = static_cast<uint8_t>(code);
-                s += mc_count[code];
+                const unsigned cnt = mc_count[code];
+                s += (static_cast<unsigned long long>(cnt) << 32) | (cnt ? 1ull : 0ull);
             }
         }
         unsigned long long tot;
@@ -259,13 +284,13 @@ __global__ void __launch_bounds__(kScanThreads) mc_dense_codes_kernel(McPlan p)
         if (threadIdx.x == 0)
             p.tiles_soup[tile] = tot;
     }
-    finish_tile_sums(ntiles, p.tiles_soup, &p.ctr->scan_soup, SoupTotal{ p.ctr });
+    finish_tile_sums(ntiles, p.tiles_soup, &p.ctr->scan_soup, PackedTotal{ p.ctr });
 }
 
 // Pass 2, over the same tiles with kScanItems consecutive points per thread
-// (one 8-byte read of codes, one block scan per tile): the active cells' soup.
-template <int DT, bool WIDE>
-__global__ void __launch_bounds__(kScanThreads) mc_dense_emit_kernel(McPlan p, float* __restrict__ verts, int64_t* __restrict__ faces)
+// (one 8-byte read of codes, one block scan per tile): every active cell and
+// its first soup vertex into the active list, in cell order.
+__global__ void __launch_bounds__(kScanThreads) mc_dense_compact_kernel(McPlan p)
 {
     static_assert(kScanItems == 8, "one 8-byte read of codes per thread");
     const int64_t ntiles = (p.points + kScanTile - 1) / kScanTile;
@@ -287,53 +312,83 @@ __global__ void __launch_bounds__(kScanThreads) mc_dense_emit_kernel(McPlan p, f
         unsigned long long s = 0;
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k)
-            s += mc_count[((k < 4 ? lo : hi) >> (8 * (k & 3))) & 0xffu];
+        {
+            const unsigned cnt = mc_count[((k < 4 ? lo : hi) >> (8 * (k & 3))) & 0xffu];
+            s += (static_cast<unsigned long long>(cnt) << 32) | (cnt ? 1ull : 0ull);
+        }
         unsigned long long tot;
         unsigned long long off = block_exclusive_scan(s, &tot) + p.tiles_soup[tile];
         if (s == 0)
             continue;
+#pragma unroll
         for (int k = 0; k < kScanItems; ++k)
         {
-            const int code = static_cast<int>(((k < 4 ? lo : hi) >> (8 * (k & 3))) & 0xffu);
-            const int cnt = mc_count[code];
+            const unsigned cnt = mc_count[((k < 4 ? lo : hi) >> (8 * (k & 3))) & 0xffu];
             if (cnt)
             {
-                dense_emit_cell<DT, WIDE>(p, base + k, code, off, cnt, verts, faces);
-                off += cnt;
+                const unsigned long long a = off & 0xffffffffull;
+                p.active[a] = base + k;
+                p.active_soup[a] = off >> 32;
+                off += (static_cast<unsigned long long>(cnt) << 32) | 1ull;
             }
         }
     }
 }
 
-// The unique vertices, in edge-id order (one warp per group of 32 points).
+// The soup of every active cell, one thread per cell.
+template <int DT, bool WIDE>
+__global__ void __launch_bounds__(256) mc_dense_faces_kernel(McPlan p, float* __restrict__ verts, int64_t* __restrict__ faces)
+{
+    const int64_t n = static_cast<int64_t>(p.ctr->active);
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        const int64_t q = p.active[i];
+        const int code = p.codes[q];
+        dense_emit_cell<DT, WIDE>(p, q, code, p.active_soup[i], mc_count[code], verts, faces);
+    }
+}
+
+// The unique vertices, in edge-id order (one warp per group of 32 points,
+// four groups per iteration).
 template <int DT, bool WIDE>
 __global__ void __launch_bounds__(256) mc_dense_verts_kernel(McPlan p, float* __restrict__ verts)
 {
+    constexpr int kGroups = 4;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     const int64_t WH = p.W * p.H;
-    for (int64_t g = warp; g < p.ngroups; g += nwarps)
+    const uint32_t bit = 1u << lane, lt = bit - 1u;
+    for (int64_t g0 = warp; g0 < p.ngroups; g0 += kGroups * nwarps)
     {
-        const McGroup e = p.groups[g];
-        const uint32_t bit = 1u << lane;
-        const uint32_t mine = ((e.x & bit) ? 1u : 0u) | ((e.y & bit) ? 2u : 0u) | ((e.z & bit) ? 4u : 0u);
-        if (!mine)
-            continue;
-        const uint32_t lt = bit - 1u;
-        unsigned long long r = e.base + __popc(e.x & lt) + __popc(e.y & lt) + __popc(e.z & lt);
-        const int64_t q = g * 32 + lane;
-        int64_t x, y, z;
-        decode<WIDE>(p, q, x, y, z);
-        const float v1 = load_f32<DT>(p.volume, q);
+        McGroup e[kGroups];
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+        for (int j = 0; j < kGroups; ++j)
         {
-            if (!((mine >> a) & 1u))
+            const int64_t g = g0 + j * nwarps;
+            e[j] = g < p.ngroups ? p.groups[g] : McGroup{ 0u, 0u, 0u, 0u, 0ull };
+        }
+#pragma unroll
+        for (int j = 0; j < kGroups; ++j)
+        {
+            const uint32_t mine = ((e[j].x & bit) ? 1u : 0u) | ((e[j].y & bit) ? 2u : 0u) | ((e[j].z & bit) ? 4u : 0u);
+            if (!mine)
                 continue;
-            const int64_t q2 = q + (a == 0 ? 1 : (a == 1 ? p.W : WH));
-            mc_vertex(p, x, y, z, a, v1, load_f32<DT>(p.volume, q2), verts + 3 * r);
-            ++r;
+            unsigned long long r = e[j].base + __popc(e[j].x & lt) + __popc(e[j].y & lt) + __popc(e[j].z & lt);
+            const int64_t q = (g0 + j * nwarps) * 32 + lane;
+            int64_t x, y, z;
+            decode<WIDE>(p, q, x, y, z);
+            const float v1 = load_f32<DT>(p.volume, q);
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+            {
+                if (!((mine >> a) & 1u))
+                    continue;
+                const int64_t q2 = q + (a == 0 ? 1 : (a == 1 ? p.W : WH));
+                mc_vertex(p, x, y, z, a, v1, load_f32<DT>(p.volume, q2), verts + 3 * r);
+                ++r;
+            }
         }
     }
 }
@@ -596,7 +651,9 @@ void dense_emit(const McPlan& p, float* verts, int64_t* faces, cudaStream_t s)
         mc_dense_verts_kernel<DT, WIDE><<<grid_for(p.ngroups * 32, 256), 256, 0, s>>>(p, verts);
         TH_LAUNCH_CHECK();
     }
-    mc_dense_emit_kernel<DT, WIDE><<<dense_grid(p), kScanThreads, 0, s>>>(p, verts, faces);
+    mc_dense_compact_kernel<<<dense_grid(p), kScanThreads, 0, s>>>(p);
+    TH_LAUNCH_CHECK();
+    mc_dense_faces_kernel<DT, WIDE><<<grid_for(p.nactive, 256), 256, 0, s>>>(p, verts, faces);
     TH_LAUNCH_CHECK();
 }
 

@@ -17,8 +17,9 @@ enum McFlags : unsigned int
 
 struct McCounters
 {
-    unsigned long long soup;  // soup vertices, 3 per face
-    unsigned long long verts; // unique vertices
+    unsigned long long soup;   // soup vertices, 3 per face
+    unsigned long long verts;  // unique vertices
+    unsigned long long active; // active cells (dense volumes)
     unsigned int flags;       // McFlags
     unsigned int pad;
     ScanState scan_soup;
@@ -58,6 +59,9 @@ struct McPlan
     unsigned long long* vbase; // sparse, unique: first vertex of each entry
     unsigned long long* tiles_soup;
     unsigned long long* tiles_verts;
+    int64_t* active;                 // dense: active cells (base points), ascending
+    unsigned long long* active_soup; // dense: their first soup vertex
+    int64_t nactive;                 // dense: active cells (known after phase 1)
     McCounters* ctr;
 };
 
