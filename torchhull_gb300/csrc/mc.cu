@@ -120,17 +120,21 @@ __global__ void __launch_bounds__(256) mc_dense_edges_kernel(McPlan p)
 #pragma unroll
         for (int j = 0; j < kGroups; ++j)
         {
+            // unconditional loads at indices clamped into the volume, so that
+            // all groups' loads are in flight together
             const int64_t q = (g0 + j * nwarps) * 32 + lane;
-            ex[j] = ey[j] = ez[j] = false;
-            if (q < p.points)
-            {
-                int64_t x, y, z;
-                decode<WIDE>(p, q, x, y, z);
-                const bool b = below<DT>(p.volume, q, p.iso);
-                ex[j] = x + 1 < p.W && below<DT>(p.volume, q + 1, p.iso) != b;
-                ey[j] = y + 1 < p.H && below<DT>(p.volume, q + p.W, p.iso) != b;
-                ez[j] = z + 1 < p.D && below<DT>(p.volume, q + WH, p.iso) != b;
-            }
+            const int64_t last = p.points - 1;
+            const int64_t qc = q < last ? q : last;
+            int64_t x, y, z;
+            decode<WIDE>(p, qc, x, y, z);
+            const bool b = below<DT>(p.volume, qc, p.iso);
+            const bool bx = below<DT>(p.volume, qc + 1 < last ? qc + 1 : last, p.iso);
+            const bool by = below<DT>(p.volume, qc + p.W < last ? qc + p.W : last, p.iso);
+            const bool bz = below<DT>(p.volume, qc + WH < last ? qc + WH : last, p.iso);
+            const bool in = q < p.points;
+            ex[j] = in && x + 1 < p.W && bx != b;
+            ey[j] = in && y + 1 < p.H && by != b;
+            ez[j] = in && z + 1 < p.D && bz != b;
         }
 #pragma unroll
         for (int j = 0; j < kGroups; ++j)
@@ -209,19 +213,23 @@ __device__ __forceinline__ unsigned long long dense_vertex(const McGroup* groups
 
 // Cell code of the cell with base point q (classify_voxels_dense :146-178),
 // -1 if q is on the last slice of an axis.  Bit i: corner i is below the isolevel.
+// The loads are unconditional (indices clamped into the volume) so that the
+// loads of several points are in flight together.
 template <int DT, bool WIDE>
 __device__ __forceinline__ int dense_code(const McPlan& p, int64_t q, int64_t& x, int64_t& y, int64_t& z)
 {
     decode<WIDE>(p, q, x, y, z);
-    if (!(x + 1 < p.W && y + 1 < p.H && z + 1 < p.D))
-        return -1;
-    const int64_t WH = p.W * p.H;
+    const bool cell = x + 1 < p.W && y + 1 < p.H && z + 1 < p.D;
+    const int64_t WH = p.W * p.H, last = p.points - 1;
     int code = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i)
-        if (below<DT>(p.volume, q + (i & 1) + ((i >> 1) & 1) * p.W + ((i >> 2) & 1) * WH, p.iso))
+    {
+        const int64_t c = q + (i & 1) + ((i >> 1) & 1) * p.W + ((i >> 2) & 1) * WH;
+        if (below<DT>(p.volume, c < last ? c : last, p.iso))
             code |= 1 << i;
-    return code;
+    }
+    return cell ? code : -1;
 }
 
 // Soup of the active cell with base point q and code (generate_faces_dense
@@ -265,17 +273,24 @@ __global__ void __launch_bounds__(kScanThreads) mc_dense_codes_kernel(McPlan p)
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
     {
         unsigned long long s = 0;
+        int codes[kScanItems];
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+        {
+            // clamped, so that every round's loads issue before any result is used
+            const int64_t q = tile * kScanTile + k * kScanThreads + threadIdx.x;
+            int64_t x, y, z;
+            const int c = dense_code<DT, WIDE>(p, q < p.points ? q : p.points - 1, x, y, z);
+            codes[k] = c < 0 ? 0 : c;
+        }
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k)
         {
             const int64_t q = tile * kScanTile + k * kScanThreads + threadIdx.x;
             if (q < p.points)
             {
-                int64_t x, y, z;
-                const int c = dense_code<DT, WIDE>(p, q, x, y, z);
-                const int code = c < 0 ? 0 : c;
-                p.codes[q] = static_cast<uint8_t>(code);
-                const unsigned cnt = mc_count[code];
+                p.codes[q] = static_cast<uint8_t>(codes[k]);
+                const unsigned cnt = mc_count[codes[k]];
                 s += (static_cast<unsigned long long>(cnt) << 32) | (cnt ? 1ull : 0ull);
             }
         }
