@@ -26,7 +26,7 @@ def alone(th, r):
     return v.cpu(), f.cpu()
 
 
-@pytest.mark.parametrize("priority", ["large_first", "small_first", "none"])
+@pytest.mark.parametrize("priority", ["exclusive_large", "large_first", "small_first", "none"])
 def test_results_in_the_mix_equal_results_alone(th, cuda, requests, priority):
     from torchhull_gb300.serve import HullServer
 

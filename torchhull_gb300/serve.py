@@ -67,12 +67,14 @@ class _Job:
 class HullServer:
     """Continuous-batching visual-hull server on one device."""
 
-    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: float = 60e9, priority: str = "large_first",
+    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: float = 60e9, priority: str = "exclusive_large",
                  large_bytes: float = 2e9):
-        """priority: which requests run on high-priority CUDA streams, so that the block scheduler
-        prefers their kernels while others are running: "large_first" (requests whose estimated
-        device memory exceeds large_bytes; they set the tail latency), "small_first", or "none"."""
-        if priority not in ("large_first", "small_first", "none"):
+        """priority: how requests above large_bytes of estimated device memory (the ones that set
+        the tail latency) share the GPU.  "exclusive_large": a large request waits until the
+        running ones finish and then runs alone, and nothing is admitted while it waits or runs;
+        "large_first" / "small_first": large / small requests run on high-priority CUDA streams,
+        so the block scheduler prefers their kernels; "none": all requests alike."""
+        if priority not in ("exclusive_large", "large_first", "small_first", "none"):
             raise ValueError(f"unknown priority policy {priority!r}")
         self.device = torch.device("cuda", device)
         self.budget = int(budget_bytes)
@@ -82,6 +84,7 @@ class HullServer:
         self._pending: collections.deque[_Job] = collections.deque()
         self._in_flight = 0
         self._running_bytes = 0
+        self._large_running = False
         self._closed = False
         self.latencies_ms: list[float] = []
         self.queue_ms: list[float] = []
@@ -133,9 +136,21 @@ class HullServer:
                 "pool_bytes": sum(c.device_bytes() for c in self._contexts)}
 
     # -- server side ---------------------------------------------------------
+    def _is_large(self, job: _Job) -> bool:
+        return job.bytes > self.large_bytes
+
     def _admit(self) -> _Job | None:
         """First pending job that fits the budget (called with the lock held)."""
+        exclusive = self.priority == "exclusive_large"
+        if exclusive and self._large_running:
+            return None
         for i, job in enumerate(self._pending):
+            if exclusive and self._is_large(job):
+                if self._in_flight > 0:
+                    return None  # drain the running requests, admit nothing meanwhile
+                del self._pending[i]
+                self._large_running = True
+                return job
             if self._running_bytes + job.bytes <= self.budget or self._in_flight == 0:
                 del self._pending[i]
                 return job
@@ -179,4 +194,6 @@ class HullServer:
                 with self._cv:
                     self._in_flight -= 1
                     self._running_bytes -= job.bytes
+                    if self.priority == "exclusive_large" and self._is_large(job):
+                        self._large_running = False
                     self._cv.notify_all()
