@@ -292,7 +292,12 @@ typedef enum th_option
      * each size/level/mode signature is run with both kernels and the faster
      * choice is kept), 1 = views over lanes everywhere, 2 = (parent, view) work
      * items from level 4 on. */
-    TH_OPTION_CARVE_KERNEL = 1
+    TH_OPTION_CARVE_KERNEL = 1,
+    /* 1 (default): th_visual_hull replays the octree, corner, field and
+     * marching-cubes stages of a request as a CUDA graph captured once per
+     * request shape (sizes, level, modes, dtype, pools); 0: launches them
+     * one by one.  Profiled and autotuning runs always launch directly. */
+    TH_OPTION_GRAPHS = 2
 } th_option;
 th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value);
 th_status th_context_stage_times(const th_context* ctx, th_stage_times* out);

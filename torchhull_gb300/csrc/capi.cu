@@ -32,9 +32,17 @@ namespace
 std::atomic<int64_t> g_launches{ 0 };
 }
 
+// Kernels enqueued while this thread captures a graph are counted when the
+// graph is replayed, not when captured.
+thread_local bool t_capturing = false;
+thread_local int64_t t_captured = 0;
+
 void note_launches(int n)
 {
-    g_launches.fetch_add(n, std::memory_order_relaxed);
+    if (t_capturing)
+        t_captured += n;
+    else
+        g_launches.fetch_add(n, std::memory_order_relaxed);
 }
 
 void check_launch(const char* what)
@@ -121,25 +129,52 @@ struct HullSlot
     int64_t node_cap = 0, corner_cap = 0, parent_cap = 0;
     HullPlan plan{};
     DevCounters* host = nullptr; // pinned copy of the counters
+    DevBuf rq;                   // ReqConsts of the running request (device)
+    ReqConsts* host_rq = nullptr; // pinned source of rq
     th_hull_info info{};
     bool has_result = false;
     bool dirty = false; // bitmap rows of the last request still set
     cudaEvent_t done = nullptr;
 
+    // Captured pipelines, keyed by the plan with the per-request fields cleared.
+    struct Graph
+    {
+        HullPlan key;
+        cudaGraphExec_t exec = nullptr;
+        int64_t kernels = 0;
+    };
+    std::vector<Graph> graphs;
+    cudaStream_t capture_stream = nullptr; // capture only (graphs launch on the caller's stream)
+
+    void drop_graphs()
+    {
+        for (auto& g : graphs)
+            if (g.exec)
+                cudaGraphExecDestroy(g.exec);
+        graphs.clear();
+    }
+
     std::vector<const DevBuf*> buffers() const
     {
         return { &tf,     &sat,  &nodes,    &node_skip, &child_masks, &child_skip, &tile_sums,
                  &bitmap, &word_rank, &rowbits, &rows, &corners,    &values,     &codes,
-                 &emask,  &soup_off, &vbase,   &counters, &flags };
+                 &emask,  &soup_off, &vbase,   &counters, &flags, &rq };
     }
 
     void release()
     {
+        drop_graphs();
         for (const DevBuf* b : buffers())
             const_cast<DevBuf*>(b)->release();
         if (host)
             cudaFreeHost(host);
         host = nullptr;
+        if (host_rq)
+            cudaFreeHost(host_rq);
+        host_rq = nullptr;
+        if (capture_stream)
+            cudaStreamDestroy(capture_stream);
+        capture_stream = nullptr;
         if (done)
             cudaEventDestroy(done);
         done = nullptr;
@@ -313,6 +348,7 @@ struct th_context
     th::StageEvents events;
     th_stage_times times{};
     int carve_mode = 0; // TH_OPTION_CARVE_KERNEL
+    bool graphs = true;  // TH_OPTION_GRAPHS
     std::map<th::TuneKey, th::CarveVariants> carve_tuned;
     cudaEvent_t tune_ev[2] = { nullptr, nullptr };
 };
@@ -443,7 +479,7 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool batch_slo
         TH_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
 
     HullPlan& p = s.plan;
-    p = HullPlan{};
+    std::memset(&p, 0, sizeof(HullPlan)); // zero padding too: plans are compared bytewise
     p.masks = a->masks;
     p.masks_dtype = a->masks_dtype;
     p.B = B;
@@ -483,6 +519,13 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool batch_slo
     p.vbase = s.vbase.as<uint32_t>();
     p.corner_cap = corner_cap;
     p.ctr = s.counters.as<DevCounters>();
+    // the per-request inputs the carve and field kernels read from the device
+    s.rq.ensure(sizeof(ReqConsts));
+    if (!s.host_rq)
+        TH_CUDA(cudaMallocHost(&s.host_rq, sizeof(ReqConsts)));
+    *s.host_rq = ReqConsts{ { p.corner[0], p.corner[1], p.corner[2] }, p.length, p.masks };
+    TH_CUDA(cudaMemcpyAsync(s.rq.p, s.host_rq, sizeof(ReqConsts), cudaMemcpyHostToDevice, st));
+    p.rq = s.rq.as<ReqConsts>();
 }
 
 void fill_info(const HullSlot& s, th_hull_info* info)
@@ -514,6 +557,94 @@ void fill_info(const HullSlot& s, th_hull_info* info)
         out.num_faces = c.soup / 3;
     }
     *info = out;
+}
+
+// Everything of a run after the integral image: octree levels, corners,
+// field, marching cubes and the read-back of the counters (stream-ordered
+// only, so that it can be captured as a graph).
+void enqueue_core(th_context* ctx, HullSlot& s, cudaStream_t st, StageEvents* ev, bool tune)
+{
+    const HullPlan& p = s.plan;
+    const int L = p.level;
+    launch_hull_init(p, st);
+    // With an empty image every child is empty in the first view (the
+    // reference samples zeros everywhere), so the octree stops at the root;
+    // without views nothing is refined either.  Skip the carve in both cases.
+    const bool carve = p.B > 0 && p.H > 0 && p.W > 0;
+    if (tune)
+        TH_CUDA(cudaEventRecord(ctx->tune_ev[0], st));
+    for (int li = 0; li < p.level; ++li)
+    {
+        if (carve)
+            launch_carve_level(p, li, st);
+        if (ev)
+            ev->record(2 + li, st);
+    }
+    if (tune)
+        TH_CUDA(cudaEventRecord(ctx->tune_ev[1], st));
+    if (ev)
+        ev->record(L + 2, st);
+    launch_corners(p, st);
+    if (ev)
+        ev->record(L + 3, st);
+    launch_field(p, st);
+    if (ev)
+        ev->record(L + 4, st);
+    launch_marching_cubes(p, st);
+    if (ev)
+        ev->record(L + 5, st);
+    TH_CUDA(cudaMemcpyAsync(s.host, p.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+}
+
+// enqueue_core as a graph: captured once per plan (the per-request corner,
+// length and masks come through p.rq, uploaded by prepare), replayed after.
+void replay_core(HullSlot& s, cudaStream_t st)
+{
+    HullPlan key;
+    std::memcpy(&key, &s.plan, sizeof(HullPlan));
+    key.masks = nullptr;
+    key.corner[0] = key.corner[1] = key.corner[2] = 0.f;
+    key.length = 0.f;
+    HullSlot::Graph* g = nullptr;
+    for (auto& e : s.graphs)
+        if (std::memcmp(&e.key, &key, sizeof(HullPlan)) == 0)
+            g = &e;
+    if (!g)
+    {
+        if (s.graphs.size() >= 8)
+            s.drop_graphs();
+        // captured on a private stream (the caller's may be the legacy
+        // default stream, which cannot capture); nothing runs while capturing
+        if (!s.capture_stream)
+            TH_CUDA(cudaStreamCreateWithFlags(&s.capture_stream, cudaStreamNonBlocking));
+        const cudaStream_t cs = s.capture_stream;
+        cudaGraph_t graph = nullptr;
+        TH_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        t_capturing = true;
+        t_captured = 0;
+        try
+        {
+            enqueue_core(nullptr, s, cs, nullptr, false);
+        }
+        catch (...)
+        {
+            t_capturing = false;
+            cudaStreamEndCapture(cs, &graph);
+            if (graph)
+                cudaGraphDestroy(graph);
+            throw;
+        }
+        t_capturing = false;
+        TH_CUDA(cudaStreamEndCapture(cs, &graph));
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        TH_CUDA(e);
+        s.graphs.push_back(HullSlot::Graph{ key, exec, t_captured });
+        g = &s.graphs.back();
+    }
+    TH_CUDA(cudaGraphLaunch(g->exec, st));
+    note_launches(static_cast<int>(g->kernels));
 }
 
 // One complete run of a request with the given carve kernels.  carve_ms
@@ -551,34 +682,10 @@ void run_hull_once(th_context* ctx,
             if (ev)
                 ev->record(1, st);
         }
-        launch_hull_init(p, st);
-        // With an empty image every child is empty in the first view (the
-        // reference samples zeros everywhere), so the octree stops at the root;
-        // without views nothing is refined either.  Skip the carve in both cases.
-        const bool carve = p.B > 0 && p.H > 0 && p.W > 0;
-        if (carve_ms)
-            TH_CUDA(cudaEventRecord(ctx->tune_ev[0], st));
-        for (int li = 0; li < p.level; ++li)
-        {
-            if (carve)
-                launch_carve_level(p, li, st);
-            if (ev)
-                ev->record(2 + li, st);
-        }
-        if (carve_ms)
-            TH_CUDA(cudaEventRecord(ctx->tune_ev[1], st));
-        if (ev)
-            ev->record(L + 2, st);
-        launch_corners(p, st);
-        if (ev)
-            ev->record(L + 3, st);
-        launch_field(p, st);
-        if (ev)
-            ev->record(L + 4, st);
-        launch_marching_cubes(p, st);
-        if (ev)
-            ev->record(L + 5, st);
-        TH_CUDA(cudaMemcpyAsync(s.host, p.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+        if (ctx->graphs && !ev && !carve_ms)
+            replay_core(s, st);
+        else
+            enqueue_core(ctx, s, st, ev, carve_ms != nullptr);
         TH_CUDA(cudaStreamSynchronize(st));
         s.dirty = true;
         const int64_t ovf = s.host->overflow;
@@ -1137,9 +1244,12 @@ int64_t th_context_device_bytes(const th_context* ctx)
 th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value)
 {
     return guarded(ctx, [&] {
-        if (option != TH_OPTION_CARVE_KERNEL || value < 0 || value > 2)
+        if (option == TH_OPTION_CARVE_KERNEL && value >= 0 && value <= 2)
+            ctx->carve_mode = static_cast<int>(value);
+        else if (option == TH_OPTION_GRAPHS && (value == 0 || value == 1))
+            ctx->graphs = value != 0;
+        else
             throw ArgError{ TH_ERR_INVALID_ARGUMENT, "unknown option or value" };
-        ctx->carve_mode = static_cast<int>(value);
     });
 }
 

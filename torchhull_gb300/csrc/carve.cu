@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_views_kernel
         if (valid)
         {
             float wx[3], wy[3], wz[3];
-            lattice_world(p.corner, p.length, L.parents[pi], li, L.inv_rc, wx, wy, wz);
+            lattice_world(p.rq->corner, p.rq->length, L.parents[pi], li, L.inv_rc, wx, wy, wz);
             const ViewSource src = make_view_source(p.tf, p.sat, p.H, p.W);
             for (int64_t b = sub; b < p.B; b += LANES)
             {
@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel
                 const int na = __popc(active);
                 b = j < na ? select_bit(active, j) : 32 + (j - na);
                 float wx[3], wy[3], wz[3];
-                lattice_world(p.corner, p.length, is, li, L.inv_rc, wx, wy, wz);
+                lattice_world(p.rq->corner, p.rq->length, is, li, L.inv_rc, wx, wy, wz);
                 const ViewSource src = make_view_source(p.tf, p.sat, p.H, p.W);
                 res = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, L.produce && b < 32, L.skip_inside);
             }

@@ -177,9 +177,9 @@ struct CornerEpilogue
 };
 
 template <int DT>
-__device__ __forceinline__ float mask_sample(const HullPlan& p, int64_t b, int64_t y, int64_t x, float pad)
+__device__ __forceinline__ float mask_sample(const HullPlan& p, const void* masks, int64_t b, int64_t y, int64_t x, float pad)
 {
-    return (0 <= y && y < p.H && 0 <= x && x < p.W) ? load_f32<DT>(p.masks, (b * p.H + y) * p.W + x) : pad;
+    return (0 <= y && y < p.H && 0 <= x && x < p.W) ? load_f32<DT>(masks, (b * p.H + y) * p.W + x) : pad;
 }
 
 // Factor of view b for the corner at world point (wx, wy, wz): the bilinear
@@ -195,7 +195,7 @@ __device__ __forceinline__ float mask_sample(const HullPlan& p, int64_t b, int64
 // are padding, for which the interpolation gives the same result (0, 1 or
 // NaN) for either weight.
 template <int DT, bool PARTIAL>
-__device__ __forceinline__ float view_factor(const HullPlan& p, int64_t b, float wx, float wy, float wz, float Hf, float Wf)
+__device__ __forceinline__ float view_factor(const HullPlan& p, const void* masks, int64_t b, float wx, float wy, float wz, float Hf, float Wf)
 {
     const float* m = p.tf + 16 * b;
     float px, py;
@@ -216,10 +216,10 @@ __device__ __forceinline__ float view_factor(const HullPlan& p, int64_t b, float
         rx.f = __int2float_rn(rx.i);
     }
     const int64_t y0 = ry.i, x0 = rx.i;
-    const float v00 = mask_sample<DT>(p, b, y0, x0, pad);
-    const float v10 = mask_sample<DT>(p, b, y0 + 1, x0, pad);
-    const float v01 = mask_sample<DT>(p, b, y0, x0 + 1, pad);
-    const float v11 = mask_sample<DT>(p, b, y0 + 1, x0 + 1, pad);
+    const float v00 = mask_sample<DT>(p, masks, b, y0, x0, pad);
+    const float v10 = mask_sample<DT>(p, masks, b, y0 + 1, x0, pad);
+    const float v01 = mask_sample<DT>(p, masks, b, y0, x0 + 1, pad);
+    const float v11 = mask_sample<DT>(p, masks, b, y0 + 1, x0 + 1, pad);
     const float ty = __fsub_rn(py, ry.f);
     const float tx = __fsub_rn(px, rx.f);
     return bilerp(v00, v10, v01, v11, ty, tx);
@@ -235,6 +235,8 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p)
     const int64_t R = p.R;
     const float inv_rc = __fdiv_rn(1.f, static_cast<float>(R - 1)); // exact: a power of two
     const float Hf = small_i2f(static_cast<int32_t>(p.H)), Wf = small_i2f(static_cast<int32_t>(p.W));
+    const float cx = p.rq->corner[0], cy = p.rq->corner[1], cz = p.rq->corner[2], length = p.rq->length;
+    const void* masks = p.rq->masks;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
     {
@@ -243,13 +245,13 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p)
         unpack_corner(idx, gx, gy, gz);
         // c + v/r * L fused (visual_hull_cuda.cu:444-448); v/r == v * (1/r) exactly
         // corner coordinates are at most 2^12
-        const float wx = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gx)), inv_rc), p.length, p.corner[0]);
-        const float wy = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gy)), inv_rc), p.length, p.corner[1]);
-        const float wz = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gz)), inv_rc), p.length, p.corner[2]);
+        const float wx = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gx)), inv_rc), length, cx);
+        const float wy = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gy)), inv_rc), length, cy);
+        const float wz = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gz)), inv_rc), length, cz);
         float value = 1.f;
 #pragma unroll 4
         for (int64_t b = 0; b < p.B; ++b)
-            value = __fmul_rn(value, view_factor<DT, PARTIAL>(p, b, wx, wy, wz, Hf, Wf));
+            value = __fmul_rn(value, view_factor<DT, PARTIAL>(p, masks, b, wx, wy, wz, Hf, Wf));
         p.values[t] = value;
     }
 }

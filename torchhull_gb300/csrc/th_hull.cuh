@@ -32,6 +32,16 @@ struct DevCounters
     ScanState scan;
 };
 
+// The inputs that differ between requests of one shape, read by the carve
+// and field kernels from device memory (written before each run), so that a
+// captured graph of the pipeline serves every request of that shape.
+struct ReqConsts
+{
+    float corner[3];
+    float length;
+    const void* masks;
+};
+
 // Per-request constants and buffers, passed to kernels by value.
 struct HullPlan
 {
@@ -78,6 +88,7 @@ struct HullPlan
     uint32_t* vbase;
     int64_t corner_cap;
     DevCounters* ctr;
+    const ReqConsts* rq; // corner, length and masks of the running request (device)
 };
 
 // Corner ids inside the pipeline: x | y << 21 | z << 42 (grid points < 2^21

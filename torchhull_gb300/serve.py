@@ -67,7 +67,7 @@ class _Job:
 class HullServer:
     """Continuous-batching visual-hull server on one device."""
 
-    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: float = 60e9, priority: str = "exclusive_large",
+    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: float = 60e9, priority: str = "none",
                  large_bytes: float = 2e9):
         """priority: how requests above large_bytes of estimated device memory (the ones that set
         the tail latency) share the GPU.  "exclusive_large": a large request waits until the
