@@ -104,51 +104,6 @@ __device__ __forceinline__ void decode(const McPlan& p, int64_t q, int64_t& x, i
     }
 }
 
-// Edge bits of each group of 32 points (one warp per group, four groups per
-// iteration so that their loads are in flight together).
-template <int DT, bool WIDE>
-__global__ void __launch_bounds__(256) mc_dense_edges_kernel(McPlan p)
-{
-    constexpr int kGroups = 4;
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-    const int64_t WH = p.W * p.H;
-    for (int64_t g0 = warp; g0 < p.ngroups; g0 += kGroups * nwarps)
-    {
-        bool ex[kGroups], ey[kGroups], ez[kGroups];
-#pragma unroll
-        for (int j = 0; j < kGroups; ++j)
-        {
-            // unconditional loads at indices clamped into the volume, so that
-            // all groups' loads are in flight together
-            const int64_t q = (g0 + j * nwarps) * 32 + lane;
-            const int64_t last = p.points - 1;
-            const int64_t qc = q < last ? q : last;
-            int64_t x, y, z;
-            decode<WIDE>(p, qc, x, y, z);
-            const bool b = below<DT>(p.volume, qc, p.iso);
-            const bool bx = below<DT>(p.volume, qc + 1 < last ? qc + 1 : last, p.iso);
-            const bool by = below<DT>(p.volume, qc + p.W < last ? qc + p.W : last, p.iso);
-            const bool bz = below<DT>(p.volume, qc + WH < last ? qc + WH : last, p.iso);
-            const bool in = q < p.points;
-            ex[j] = in && x + 1 < p.W && bx != b;
-            ey[j] = in && y + 1 < p.H && by != b;
-            ez[j] = in && z + 1 < p.D && bz != b;
-        }
-#pragma unroll
-        for (int j = 0; j < kGroups; ++j)
-        {
-            const int64_t g = g0 + j * nwarps;
-            const uint32_t X = __ballot_sync(0xffffffffu, ex[j]);
-            const uint32_t Y = __ballot_sync(0xffffffffu, ey[j]);
-            const uint32_t Z = __ballot_sync(0xffffffffu, ez[j]);
-            if (lane == 0 && g < p.ngroups)
-                p.groups[g] = McGroup{ X, Y, Z, 0u, 0ull };
-        }
-    }
-}
-
 struct GroupCount
 {
     const McGroup* groups;
@@ -211,27 +166,6 @@ __device__ __forceinline__ unsigned long long dense_vertex(const McGroup* groups
     return r;
 }
 
-// Cell code of the cell with base point q (classify_voxels_dense :146-178),
-// -1 if q is on the last slice of an axis.  Bit i: corner i is below the isolevel.
-// The loads are unconditional (indices clamped into the volume) so that the
-// loads of several points are in flight together.
-template <int DT, bool WIDE>
-__device__ __forceinline__ int dense_code(const McPlan& p, int64_t q, int64_t& x, int64_t& y, int64_t& z)
-{
-    decode<WIDE>(p, q, x, y, z);
-    const bool cell = x + 1 < p.W && y + 1 < p.H && z + 1 < p.D;
-    const int64_t WH = p.W * p.H, last = p.points - 1;
-    int code = 0;
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-    {
-        const int64_t c = q + (i & 1) + ((i >> 1) & 1) * p.W + ((i >> 2) & 1) * WH;
-        if (below<DT>(p.volume, c < last ? c : last, p.iso))
-            code |= 1 << i;
-    }
-    return cell ? code : -1;
-}
-
 // Soup of the active cell with base point q and code (generate_faces_dense
 // :242-306): faces into the unique vertex list, or soup vertices with
 // faces = arange.  off: the cell's first soup vertex.
@@ -261,44 +195,135 @@ __device__ __forceinline__ void dense_emit_cell(const McPlan& p, int64_t q, int 
     }
 }
 
-// Pass 1 over the points in tiles of kScanTile, each tile in kScanItems
-// rounds of kScanThreads consecutive points (coalesced corner loads, all
-// rounds in flight together): the cell code of every point into codes[] (0
-// where no cell starts) and, per tile, (soup vertices << 32) | active cells
-// into tiles_soup, then exclusive tile offsets of both.
-template <int DT, bool WIDE>
-__global__ void __launch_bounds__(kScanThreads) mc_dense_codes_kernel(McPlan p)
+// One pass over a dense volume that loads each value once: a block covers
+// 32 x 8 columns (x, y) and marches kMarchZ planes in z, exchanging the
+// below-isolevel bits of each plane (with a one-point halo in +x and +y)
+// through shared memory, double-buffered.  For every point it writes the cell
+// code (0 where no cell starts), ORs its three vertex-edge bits into the
+// group words (unique vertices), and adds (soup vertices << 32 | active cell)
+// to the sum of its 2048-point tile (one atomic per warp and tile).  groups
+// and tiles_soup are zero when it starts.
+constexpr int kMarchX = 32, kMarchY = 8, kMarchZ = 16;
+
+template <int DT>
+__device__ __forceinline__ uint8_t below_at(const McPlan& p, int64_t x, int64_t y, int64_t z)
 {
-    const int64_t ntiles = (p.points + kScanTile - 1) / kScanTile;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
-    {
-        unsigned long long s = 0;
-        int codes[kScanItems];
-#pragma unroll
-        for (int k = 0; k < kScanItems; ++k)
+    return (x < p.W && y < p.H && z < p.D) ? (below<DT>(p.volume, x + p.W * (y + p.H * z), p.iso) ? 1 : 0) : 0;
+}
+
+template <int DT>
+__global__ void __launch_bounds__(kMarchX * kMarchY) mc_dense_march_kernel(McPlan p)
+{
+    __shared__ uint8_t plane[2][kMarchY + 1][kMarchX + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y, lane = tx;
+    const int64_t x = static_cast<int64_t>(blockIdx.x) * kMarchX + tx;
+    const int64_t y = static_cast<int64_t>(blockIdx.y) * kMarchY + ty;
+    const int64_t z0 = static_cast<int64_t>(blockIdx.z) * kMarchZ;
+    const int64_t z1 = z0 + kMarchZ < p.D ? z0 + kMarchZ : p.D;
+    const bool in = x < p.W && y < p.H;
+
+    // plane z into buffer k: own bit, and the +x / +y halo
+    auto fill = [&](int k, int64_t z) {
+        plane[k][ty][tx] = below_at<DT>(p, x, y, z);
+        if (tx == kMarchX - 1)
+            plane[k][ty][kMarchX] = below_at<DT>(p, x + 1, y, z);
+        if (ty == kMarchY - 1)
         {
-            // clamped, so that every round's loads issue before any result is used
-            const int64_t q = tile * kScanTile + k * kScanThreads + threadIdx.x;
-            int64_t x, y, z;
-            const int c = dense_code<DT, WIDE>(p, q < p.points ? q : p.points - 1, x, y, z);
-            codes[k] = c < 0 ? 0 : c;
+            plane[k][kMarchY][tx] = below_at<DT>(p, x, y + 1, z);
+            if (tx == kMarchX - 1)
+                plane[k][kMarchY][kMarchX] = below_at<DT>(p, x + 1, y + 1, z);
         }
-#pragma unroll
-        for (int k = 0; k < kScanItems; ++k)
+    };
+    fill(0, z0);
+    __syncthreads();
+    int cur = 0;
+    for (int64_t z = z0; z < z1; ++z)
+    {
+        const int nxt = cur ^ 1;
+        if (z + 1 < p.D)
+            fill(nxt, z + 1);
+        else
         {
-            const int64_t q = tile * kScanTile + k * kScanThreads + threadIdx.x;
-            if (q < p.points)
+            plane[nxt][ty][tx] = 0;
+            if (tx == kMarchX - 1)
+                plane[nxt][ty][kMarchX] = 0;
+            if (ty == kMarchY - 1)
             {
-                p.codes[q] = static_cast<uint8_t>(codes[k]);
-                const unsigned cnt = mc_count[codes[k]];
-                s += (static_cast<unsigned long long>(cnt) << 32) | (cnt ? 1ull : 0ull);
+                plane[nxt][kMarchY][tx] = 0;
+                if (tx == kMarchX - 1)
+                    plane[nxt][kMarchY][kMarchX] = 0;
             }
         }
-        unsigned long long tot;
-        block_exclusive_scan(s, &tot);
-        if (threadIdx.x == 0)
-            p.tiles_soup[tile] = tot;
+        __syncthreads();
+        const uint32_t b0 = plane[cur][ty][tx], bx = plane[cur][ty][tx + 1];
+        const uint32_t by = plane[cur][ty + 1][tx], bxy = plane[cur][ty + 1][tx + 1];
+        const uint32_t c0 = plane[nxt][ty][tx], cx = plane[nxt][ty][tx + 1];
+        const uint32_t cy = plane[nxt][ty + 1][tx], cxy = plane[nxt][ty + 1][tx + 1];
+        const int64_t q = x + p.W * (y + p.H * z);
+        // corner i = (i & 1, i >> 1 & 1, i >> 2 & 1)
+        const int code = static_cast<int>(b0 | (bx << 1) | (by << 2) | (bxy << 3) | (c0 << 4) | (cx << 5) | (cy << 6) |
+                                          (cxy << 7));
+        const bool cell = in && x + 1 < p.W && y + 1 < p.H && z + 1 < p.D;
+        const unsigned cnt = cell ? mc_count[code] : 0u;
+        if (in)
+            p.codes[q] = static_cast<uint8_t>(cell ? code : 0);
+        // the warp's 32 points are consecutive in ravel order (or end at the row's end)
+        const int64_t q0 = __shfl_sync(0xffffffffu, q, 0);
+        unsigned long long packed = (static_cast<unsigned long long>(cnt) << 32) | (cnt ? 1ull : 0ull);
+        const int64_t t0 = q0 >> 11;
+        const bool second = in && (q >> 11) != t0;
+        unsigned long long a0 = second ? 0ull : packed, a1 = second ? packed : 0ull;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1)
+        {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, d);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, d);
+        }
+        if (lane == 0)
+        {
+            if (a0)
+                atomicAdd(&p.tiles_soup[t0], a0);
+            if (a1)
+                atomicAdd(&p.tiles_soup[t0 + 1], a1);
+        }
+        if (p.unique)
+        {
+            const bool ex = in && x + 1 < p.W && bx != b0;
+            const bool ey = in && y + 1 < p.H && by != b0;
+            const bool ez = in && z + 1 < p.D && c0 != b0;
+            const uint32_t X = __ballot_sync(0xffffffffu, ex), Y = __ballot_sync(0xffffffffu, ey),
+                           Z = __ballot_sync(0xffffffffu, ez);
+            if (lane == 0)
+            {
+                const int64_t g0 = q0 >> 5;
+                const int sh = static_cast<int>(q0 & 31);
+                McGroup& G0 = p.groups[g0];
+                if (X << sh)
+                    atomicOr(&G0.x, X << sh);
+                if (Y << sh)
+                    atomicOr(&G0.y, Y << sh);
+                if (Z << sh)
+                    atomicOr(&G0.z, Z << sh);
+                if (sh)
+                {
+                    McGroup& G1 = p.groups[g0 + 1];
+                    if (X >> (32 - sh))
+                        atomicOr(&G1.x, X >> (32 - sh));
+                    if (Y >> (32 - sh))
+                        atomicOr(&G1.y, Y >> (32 - sh));
+                    if (Z >> (32 - sh))
+                        atomicOr(&G1.z, Z >> (32 - sh));
+                }
+            }
+        }
+        cur = nxt;
+        __syncthreads(); // plane[cur ^ 1] is refilled next
     }
+}
+
+// The tile sums of the march into exclusive offsets (one block).
+__global__ void __launch_bounds__(kScanThreads) mc_dense_tiles_kernel(McPlan p, int64_t ntiles)
+{
     finish_tile_sums(ntiles, p.tiles_soup, &p.ctr->scan_soup, PackedTotal{ p.ctr });
 }
 
@@ -647,15 +672,20 @@ int dense_grid(const McPlan& p)
 template <int DT, bool WIDE>
 void dense_count(const McPlan& p, cudaStream_t s)
 {
+    const int64_t ntiles = (p.points + kScanTile - 1) / kScanTile;
+    TH_CUDA(cudaMemsetAsync(p.tiles_soup, 0, sizeof(unsigned long long) * ntiles, s));
     if (p.unique)
-    {
-        mc_dense_edges_kernel<DT, WIDE><<<grid_for(p.ngroups * 32, 256), 256, 0, s>>>(p);
-        TH_LAUNCH_CHECK();
+        TH_CUDA(cudaMemsetAsync(p.groups, 0, sizeof(McGroup) * p.ngroups, s));
+    const dim3 grid(static_cast<unsigned>((p.W + kMarchX - 1) / kMarchX),
+                    static_cast<unsigned>((p.H + kMarchY - 1) / kMarchY),
+                    static_cast<unsigned>((p.D + kMarchZ - 1) / kMarchZ));
+    mc_dense_march_kernel<DT><<<grid, dim3(kMarchX, kMarchY), 0, s>>>(p);
+    TH_LAUNCH_CHECK();
+    mc_dense_tiles_kernel<<<1, kScanThreads, 0, s>>>(p, ntiles);
+    TH_LAUNCH_CHECK();
+    if (p.unique)
         run_scan(GroupCount{ p.groups }, GroupEmit{ p.groups }, VertTotal{ p.ctr }, Count{ nullptr, p.ngroups },
                  p.ngroups, p.tiles_verts, &p.ctr->scan_verts, s);
-    }
-    mc_dense_codes_kernel<DT, WIDE><<<dense_grid(p), kScanThreads, 0, s>>>(p);
-    TH_LAUNCH_CHECK();
 }
 
 template <int DT, bool WIDE>
