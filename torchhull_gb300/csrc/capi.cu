@@ -349,6 +349,7 @@ struct th_context
     th_stage_times times{};
     int carve_mode = 0; // TH_OPTION_CARVE_KERNEL
     bool graphs = true;  // TH_OPTION_GRAPHS
+    bool batch_route = true; // TH_OPTION_BATCH_ROUTE
     std::map<th::TuneKey, th::CarveVariants> carve_tuned;
     cudaEvent_t tune_ev[2] = { nullptr, nullptr };
 };
@@ -954,6 +955,47 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
     }
 }
 
+// A request whose octree alone fills the GPU (level >= 8 and at least 16 M
+// mask pixels) gains nothing from sharing launches and runs through the
+// per-request pipeline (graph replay, autotuned carve kernels; the
+// persistent carve was 6-27 % slower on such requests); the others share the
+// persistent carve.  Results are identical either way.
+bool fills_gpu(const th_hull_args& a)
+{
+    return a.level >= 8 && a.batch * a.height * a.width >= (int64_t{ 1 } << 24);
+}
+
+void run_batch_routed(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_t st, th_hull_info* infos)
+{
+    for (int32_t r = 0; r < n; ++r)
+        validate(&args[r]);
+    std::vector<int32_t> shared, solo;
+    for (int32_t r = 0; r < n; ++r)
+        (ctx->batch_route && fills_gpu(args[r]) ? solo : shared).push_back(r);
+    if (static_cast<int32_t>(ctx->batch.size()) < n)
+        ctx->batch.resize(n);
+    if (!shared.empty())
+    {
+        std::vector<th_hull_args> sub(shared.size());
+        std::vector<th_hull_info> sub_infos(shared.size());
+        for (size_t j = 0; j < shared.size(); ++j)
+            sub[j] = args[shared[j]];
+        run_batch(ctx, sub.data(), static_cast<int32_t>(sub.size()), st, sub_infos.data());
+        // results of shared[j] sit in slot j <= shared[j]: move them into place,
+        // last first, so no placed result is moved again
+        for (size_t j = shared.size(); j-- > 0;)
+        {
+            std::swap(ctx->batch[j], ctx->batch[shared[j]]);
+            infos[shared[j]] = sub_infos[j];
+        }
+    }
+    for (int32_t r : solo)
+    {
+        run_hull(ctx, ctx->batch[r], &args[r], st, nullptr);
+        infos[r] = ctx->batch[r].info;
+    }
+}
+
 th_status fail(th_context* ctx, th_status st, const std::string& msg)
 {
     if (ctx)
@@ -1248,6 +1290,8 @@ th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value)
             ctx->carve_mode = static_cast<int>(value);
         else if (option == TH_OPTION_GRAPHS && (value == 0 || value == 1))
             ctx->graphs = value != 0;
+        else if (option == TH_OPTION_BATCH_ROUTE && (value == 0 || value == 1))
+            ctx->batch_route = value != 0;
         else
             throw ArgError{ TH_ERR_INVALID_ARGUMENT, "unknown option or value" };
     });
@@ -1500,7 +1544,7 @@ th_status th_visual_hull_batch(th_context* ctx, const th_hull_args* args, int32_
     return guarded(ctx, [&] {
         if (n < 0 || (n > 0 && (!args || !infos)))
             throw ArgError{ TH_ERR_INVALID_ARGUMENT, "invalid batch arguments" };
-        run_batch(ctx, args, n, static_cast<cudaStream_t>(stream), infos);
+        run_batch_routed(ctx, args, n, static_cast<cudaStream_t>(stream), infos);
     });
 }
 
