@@ -310,7 +310,7 @@ namespace
 // Pools and the last result of the public marching cubes.
 struct McSlot
 {
-    DevBuf groups, keys, slots, codes, used, vbase, tiles_soup, tiles_verts, active, active_soup, ctr;
+    DevBuf groups, keys, slots, codes, used, vbase, tiles_soup, tiles_verts, tiles_scan, active, active_soup, ctr;
     McCounters* host = nullptr; // pinned copy of the counters
     McPlan plan{};
     th_mc_info info{};
@@ -318,7 +318,8 @@ struct McSlot
 
     std::vector<const DevBuf*> buffers() const
     {
-        return { &groups, &keys, &slots, &codes, &used, &vbase, &tiles_soup, &tiles_verts, &active, &active_soup, &ctr };
+        return { &groups, &keys, &slots, &codes, &used, &vbase, &tiles_soup, &tiles_verts, &tiles_scan, &active,
+                 &active_soup, &ctr };
     }
 
     void release()
@@ -1168,7 +1169,9 @@ void run_mc(McSlot& s, const th_mc_args* a, cudaStream_t st)
     {
         s.tiles_soup.ensure(sizeof(unsigned long long) * mc_scan_tiles(p.points));
         s.codes.ensure(static_cast<size_t>(p.points));
+        s.tiles_scan.ensure(sizeof(unsigned long long) * mc_scan_tiles(mc_scan_tiles(p.points)));
         p.tiles_soup = s.tiles_soup.as<unsigned long long>();
+        p.tiles_scan = s.tiles_scan.as<unsigned long long>();
         p.codes = s.codes.as<uint8_t>();
         if (p.unique)
         {

@@ -269,22 +269,19 @@ __global__ void __launch_bounds__(kMarchX * kMarchY) mc_dense_march_kernel(McPla
             p.codes[q] = static_cast<uint8_t>(cell ? code : 0);
         // the warp's 32 points are consecutive in ravel order (or end at the row's end)
         const int64_t q0 = __shfl_sync(0xffffffffu, q, 0);
-        unsigned long long packed = (static_cast<unsigned long long>(cnt) << 32) | (cnt ? 1ull : 0ull);
+        // per warp: soup vertices (<= 480) << 16 | active cells (<= 32), for
+        // the (at most two) 2048-point tiles the warp's points fall into
+        const unsigned packed = (cnt << 16) | (cnt ? 1u : 0u);
         const int64_t t0 = q0 >> 11;
         const bool second = in && (q >> 11) != t0;
-        unsigned long long a0 = second ? 0ull : packed, a1 = second ? packed : 0ull;
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1)
-        {
-            a0 += __shfl_xor_sync(0xffffffffu, a0, d);
-            a1 += __shfl_xor_sync(0xffffffffu, a1, d);
-        }
+        const unsigned a0 = __reduce_add_sync(0xffffffffu, second ? 0u : packed);
+        const unsigned a1 = __reduce_add_sync(0xffffffffu, second ? packed : 0u);
         if (lane == 0)
         {
             if (a0)
-                atomicAdd(&p.tiles_soup[t0], a0);
+                atomicAdd(&p.tiles_soup[t0], (static_cast<unsigned long long>(a0 >> 16) << 32) | (a0 & 0xffffu));
             if (a1)
-                atomicAdd(&p.tiles_soup[t0 + 1], a1);
+                atomicAdd(&p.tiles_soup[t0 + 1], (static_cast<unsigned long long>(a1 >> 16) << 32) | (a1 & 0xffffu));
         }
         if (p.unique)
         {
@@ -321,11 +318,25 @@ __global__ void __launch_bounds__(kMarchX * kMarchY) mc_dense_march_kernel(McPla
     }
 }
 
-// The tile sums of the march into exclusive offsets (one block).
-__global__ void __launch_bounds__(kScanThreads) mc_dense_tiles_kernel(McPlan p, int64_t ntiles)
+// The tile sums of the march into exclusive offsets, in place (a scan reads
+// all counts of a thread before it writes any offset).
+struct TileCount
 {
-    finish_tile_sums(ntiles, p.tiles_soup, &p.ctr->scan_soup, PackedTotal{ p.ctr });
-}
+    const unsigned long long* tiles;
+    __device__ unsigned long long operator()(int64_t i) const
+    {
+        return tiles[i];
+    }
+};
+
+struct TileEmit
+{
+    unsigned long long* tiles;
+    __device__ void operator()(int64_t i, unsigned long long off, unsigned long long) const
+    {
+        tiles[i] = off;
+    }
+};
 
 // Pass 2, over the same tiles with kScanItems consecutive points per thread
 // (one 8-byte read of codes, one block scan per tile): every active cell and
@@ -336,6 +347,11 @@ __global__ void __launch_bounds__(kScanThreads) mc_dense_compact_kernel(McPlan p
     const int64_t ntiles = (p.points + kScanTile - 1) / kScanTile;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
     {
+        // tiles without an active cell (most of a volume) have equal offsets
+        const unsigned long long next =
+                tile + 1 < ntiles ? p.tiles_soup[tile + 1] : ((p.ctr->soup << 32) | p.ctr->active);
+        if ((next & 0xffffffffull) == (p.tiles_soup[tile] & 0xffffffffull))
+            continue;
         const int64_t base = tile * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
         uint32_t lo = 0, hi = 0;
         if (base + kScanItems <= p.points)
@@ -389,34 +405,35 @@ __global__ void __launch_bounds__(256) mc_dense_faces_kernel(McPlan p, float* __
     }
 }
 
-// The unique vertices, in edge-id order (one warp per group of 32 points,
-// four groups per iteration).
+// The unique vertices, in edge-id order.  Each lane of a warp reads one
+// group; the warp then handles its groups with vertex edges one after the
+// other, a lane per point (most groups of a volume have none).
 template <int DT, bool WIDE>
 __global__ void __launch_bounds__(256) mc_dense_verts_kernel(McPlan p, float* __restrict__ verts)
 {
-    constexpr int kGroups = 4;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     const int64_t WH = p.W * p.H;
     const uint32_t bit = 1u << lane, lt = bit - 1u;
-    for (int64_t g0 = warp; g0 < p.ngroups; g0 += kGroups * nwarps)
+    for (int64_t g0 = warp * 32; g0 < p.ngroups; g0 += nwarps * 32)
     {
-        McGroup e[kGroups];
-#pragma unroll
-        for (int j = 0; j < kGroups; ++j)
+        const int64_t gl = g0 + lane;
+        const McGroup mine_group = gl < p.ngroups ? p.groups[gl] : McGroup{ 0u, 0u, 0u, 0u, 0ull };
+        uint32_t todo = __ballot_sync(0xffffffffu, (mine_group.x | mine_group.y | mine_group.z) != 0u);
+        while (todo)
         {
-            const int64_t g = g0 + j * nwarps;
-            e[j] = g < p.ngroups ? p.groups[g] : McGroup{ 0u, 0u, 0u, 0u, 0ull };
-        }
-#pragma unroll
-        for (int j = 0; j < kGroups; ++j)
-        {
-            const uint32_t mine = ((e[j].x & bit) ? 1u : 0u) | ((e[j].y & bit) ? 2u : 0u) | ((e[j].z & bit) ? 4u : 0u);
+            const int j = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const uint32_t ex = __shfl_sync(0xffffffffu, mine_group.x, j);
+            const uint32_t ey = __shfl_sync(0xffffffffu, mine_group.y, j);
+            const uint32_t ez = __shfl_sync(0xffffffffu, mine_group.z, j);
+            const unsigned long long base = __shfl_sync(0xffffffffu, mine_group.base, j);
+            const uint32_t mine = ((ex & bit) ? 1u : 0u) | ((ey & bit) ? 2u : 0u) | ((ez & bit) ? 4u : 0u);
             if (!mine)
                 continue;
-            unsigned long long r = e[j].base + __popc(e[j].x & lt) + __popc(e[j].y & lt) + __popc(e[j].z & lt);
-            const int64_t q = (g0 + j * nwarps) * 32 + lane;
+            unsigned long long r = base + __popc(ex & lt) + __popc(ey & lt) + __popc(ez & lt);
+            const int64_t q = (g0 + j) * 32 + lane;
             int64_t x, y, z;
             decode<WIDE>(p, q, x, y, z);
             const float v1 = load_f32<DT>(p.volume, q);
@@ -681,8 +698,8 @@ void dense_count(const McPlan& p, cudaStream_t s)
                     static_cast<unsigned>((p.D + kMarchZ - 1) / kMarchZ));
     mc_dense_march_kernel<DT><<<grid, dim3(kMarchX, kMarchY), 0, s>>>(p);
     TH_LAUNCH_CHECK();
-    mc_dense_tiles_kernel<<<1, kScanThreads, 0, s>>>(p, ntiles);
-    TH_LAUNCH_CHECK();
+    run_scan(TileCount{ p.tiles_soup }, TileEmit{ p.tiles_soup }, PackedTotal{ p.ctr }, Count{ nullptr, ntiles }, ntiles,
+             p.tiles_scan, &p.ctr->scan_soup, s);
     if (p.unique)
         run_scan(GroupCount{ p.groups }, GroupEmit{ p.groups }, VertTotal{ p.ctr }, Count{ nullptr, p.ngroups },
                  p.ngroups, p.tiles_verts, &p.ctr->scan_verts, s);

@@ -179,7 +179,10 @@ struct CornerEpilogue
 template <int DT>
 __device__ __forceinline__ float mask_sample(const HullPlan& p, const void* masks, int64_t b, int64_t y, int64_t x, float pad)
 {
-    return (0 <= y && y < p.H && 0 <= x && x < p.W) ? load_f32<DT>(masks, (b * p.H + y) * p.W + x) : pad;
+    // 0 <= y < H and 0 <= x < W, as unsigned compares
+    return (static_cast<uint64_t>(y) < static_cast<uint64_t>(p.H) && static_cast<uint64_t>(x) < static_cast<uint64_t>(p.W))
+                   ? load_f32<DT>(masks, (b * p.H + y) * p.W + x)
+                   : pad;
 }
 
 // Factor of view b for the corner at world point (wx, wy, wz): the bilinear
@@ -216,20 +219,37 @@ __device__ __forceinline__ float view_factor(const HullPlan& p, const void* mask
         rx.f = __int2float_rn(rx.i);
     }
     const int64_t y0 = ry.i, x0 = rx.i;
-    const float v00 = mask_sample<DT>(p, masks, b, y0, x0, pad);
-    const float v10 = mask_sample<DT>(p, masks, b, y0 + 1, x0, pad);
-    const float v01 = mask_sample<DT>(p, masks, b, y0, x0 + 1, pad);
-    const float v11 = mask_sample<DT>(p, masks, b, y0 + 1, x0 + 1, pad);
+    float v00, v10, v01, v11;
+    if (PARTIAL)
+    {
+        // in frame: round(q - 0.5) lies in [0, size - 2], so all four samples are inside
+        const int64_t i = (b * p.H + y0) * p.W + x0;
+        v00 = load_f32<DT>(masks, i);
+        v01 = load_f32<DT>(masks, i + 1);
+        v10 = load_f32<DT>(masks, i + p.W);
+        v11 = load_f32<DT>(masks, i + p.W + 1);
+    }
+    else
+    {
+        v00 = mask_sample<DT>(p, masks, b, y0, x0, pad);
+        v10 = mask_sample<DT>(p, masks, b, y0 + 1, x0, pad);
+        v01 = mask_sample<DT>(p, masks, b, y0, x0 + 1, pad);
+        v11 = mask_sample<DT>(p, masks, b, y0 + 1, x0 + 1, pad);
+    }
     const float ty = __fsub_rn(py, ry.f);
     const float tx = __fsub_rn(px, rx.f);
     return bilerp(v00, v10, v01, v11, ty, tx);
 }
 
-// accumulate_hull_counts_{full,partial} (visual_hull_cuda.cu:419-520): all
-// views in one thread, multiplied in ascending view order; the factors of
-// consecutive views are independent, so their loads overlap.
+// accumulate_hull_counts_{full,partial} (visual_hull_cuda.cu:419-520): the
+// views [b0, b1) multiplied into each corner's running product in ascending
+// view order (b0 == 0 starts it at 1).  Views go in chunks of kFieldViews, one
+// launch each, so that all resident threads read the masks of the same few
+// views and those stay in L2; the product is the same sequence of roundings.
+constexpr int64_t kFieldViews = 16;
+
 template <int DT, bool PARTIAL>
-__global__ void __launch_bounds__(256) field_kernel(HullPlan p)
+__global__ void __launch_bounds__(256) field_kernel(HullPlan p, int64_t b0, int64_t b1)
 {
     const int64_t n = p.ctr->corners;
     const int64_t R = p.R;
@@ -248,9 +268,9 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p)
         const float wx = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gx)), inv_rc), length, cx);
         const float wy = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gy)), inv_rc), length, cy);
         const float wz = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gz)), inv_rc), length, cz);
-        float value = 1.f;
+        float value = b0 == 0 ? 1.f : p.values[t];
 #pragma unroll 4
-        for (int64_t b = 0; b < p.B; ++b)
+        for (int64_t b = b0; b < b1; ++b)
             value = __fmul_rn(value, view_factor<DT, PARTIAL>(p, masks, b, wx, wy, wz, Hf, Wf));
         p.values[t] = value;
     }
@@ -515,15 +535,20 @@ void launch_rank_corners(const HullPlan& p, cudaStream_t s)
 void launch_field(const HullPlan& p, cudaStream_t s)
 {
     const int grid = grid_for(p.corner_cap, 256);
-    bool ok = dispatch_image_dtype(p.masks_dtype, [&]<int DT>() {
-        if (p.partial)
-            field_kernel<DT, true><<<grid, 256, 0, s>>>(p);
-        else
-            field_kernel<DT, false><<<grid, 256, 0, s>>>(p);
-    });
-    if (!ok)
-        throw CudaError{ cudaErrorInvalidValue, "hull field: unsupported mask dtype" };
-    TH_LAUNCH_CHECK();
+    // at least one launch, so that B == 0 still writes the empty product 1
+    for (int64_t b0 = 0; b0 == 0 || b0 < p.B; b0 += kFieldViews)
+    {
+        const int64_t b1 = b0 + kFieldViews < p.B ? b0 + kFieldViews : p.B;
+        bool ok = dispatch_image_dtype(p.masks_dtype, [&]<int DT>() {
+            if (p.partial)
+                field_kernel<DT, true><<<grid, 256, 0, s>>>(p, b0, b1);
+            else
+                field_kernel<DT, false><<<grid, 256, 0, s>>>(p, b0, b1);
+        });
+        if (!ok)
+            throw CudaError{ cudaErrorInvalidValue, "hull field: unsupported mask dtype" };
+        TH_LAUNCH_CHECK();
+    }
 }
 
 void launch_marching_cubes(const HullPlan& p, cudaStream_t s)

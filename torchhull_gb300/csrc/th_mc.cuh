@@ -59,6 +59,7 @@ struct McPlan
     unsigned long long* vbase; // sparse, unique: first vertex of each entry
     unsigned long long* tiles_soup;
     unsigned long long* tiles_verts;
+    unsigned long long* tiles_scan; // dense: tile sums of the scan over tiles_soup
     int64_t* active;                 // dense: active cells (base points), ascending
     unsigned long long* active_soup; // dense: their first soup vertex
     int64_t nactive;                 // dense: active cells (known after phase 1)
