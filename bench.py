@@ -233,6 +233,7 @@ def run_gb300(args) -> dict | None:
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
     th._C.set_carve_kernel(local, {"auto": 0, "views": 1, "items": 2}[args.carve_kernel])
+    th._C.set_batch_route(local, args.batch_route == "on")
 
     if args.mode == "hetero":
         return finish(run_hetero(args, th, scenes, dev, world, rank), world)
@@ -623,6 +624,8 @@ def main() -> None:
     ap.add_argument("--carve-kernel", choices=["auto", "views", "items"], default="auto",
                     help="carve kernel: autotuned (default) or forced")
     ap.add_argument("--hetero-count", type=int, default=64)
+    ap.add_argument("--batch-route", choices=["on", "off"], default="on",
+                    help="batched form: requests that fill the GPU alone through the per-request pipeline")
     ap.add_argument("--mc-sizes", default="100,200,300,400,500,600", help="--mode mc: volume sizes")
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--duration", type=float, default=10.0)

@@ -3,17 +3,17 @@
 // The plain path launches a classify kernel and a compaction per level and
 // request.  Here one cooperative kernel, resident on every SM, walks the
 // levels of all requests at once: level i is one list of request-tagged cells
-// (the device work queue), grouped by request.  Warps take chunks of it
-// from an atomic head, deal the chunk's unskipped (cell, view) items to their lanes
-// with the same per-item routine as the plain kernels (th_classify.cuh), and
-// append the refined children, tagged, to a staging list with one atomic per
-// warp; after a grid-wide barrier the staged children move into the pool
-// grouped by request, and another barrier starts the next level.  Requests with different view
-// counts, sizes, levels and modes share warps; a cell whose request ends at
-// level i is a leaf and produces no items.  Children are appended in arrival
-// order, not the reference's order, which changes nothing downstream: the
-// corner set is built in a bitmap and comes out sorted either way, so each
-// request's mesh is bit-identical to the plain path's.
+// (the device work queue).  Warps take chunks of it from an atomic head,
+// deal the chunk's unskipped (cell, view) items to their lanes with the same
+// per-item routine as the plain kernels (th_classify.cuh), and record each
+// cell's refined children; after a grid-wide barrier every block writes the
+// children of a contiguous range of cells, in cell order, at offsets from a
+// grid-wide scan (two more barriers).  Lists stay in the order of the plain
+// path's compaction: requests in order, neighbouring cells together.
+// Requests with different view counts, sizes, levels and modes share warps; a
+// cell whose request ends at level i is a leaf and produces no items.  Each
+// request's mesh is bit-identical to the plain path's: the corner set is built
+// in a bitmap and comes out sorted.
 //
 // Afterwards one launch marks the corners of every request's leaves in that
 // request's bitmap; the remaining stages (corner ranks, field, marching cubes)
@@ -186,100 +186,78 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchP
                 if (q.partial && last)
                     mask &= ws.inside[lane];
             }
-            const int nch = __popc(mask);
-            const int cincl = warp_inclusive_scan(nch);
-            const int ctot = __shfl_sync(0xffffffffu, cincl, 31);
-            unsigned long long obase = 0;
-            if (lane == 0 && ctot > 0)
-                obase = atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->count[li + 1]),
-                                  static_cast<unsigned long long>(ctot));
-            obase = __shfl_sync(0xffffffffu, obase, 0);
-            // children per request: one atomic when the chunk is one request's
+            if (valid)
             {
-                unsigned long long* rc = bp.req_count + static_cast<int64_t>(li + 1) * bp.nreq;
-                const int rq = static_cast<int>(node >> kTagShift);
-                const int r0 = __shfl_sync(0xffffffffu, rq, 0);
-                if (__all_sync(0xffffffffu, nch == 0 || rq == r0))
+                // the children come out in phase B, in parent order
+                bp.child_masks[pi] = static_cast<uint8_t>(mask);
+                if (pi < bp.skip_cap)
                 {
-                    if (lane == 0 && ctot > 0)
-                        atomicAdd(&rc[r0], static_cast<unsigned long long>(ctot));
-                }
-                else if (nch)
-                {
-                    atomicAdd(&rc[rq], static_cast<unsigned long long>(nch));
-                }
-            }
-            if (nch)
-            {
-                const bool produce_me = skips && (li + 1 < q.level);
-                const int64_t cell = node & kCellMask;
-                const int64_t m = (int64_t{ 1 } << li) - 1;
-                const int64_t gx = 2 * (cell & m), gy = 2 * ((cell >> li) & m), gz = 2 * (cell >> (2 * li));
-                const int sh = li + 1;
-                const int64_t tag = node & ~kCellMask;
-                int64_t out = static_cast<int64_t>(obase) + (cincl - nch);
+                    const bool produce_me = skips && (li + 1 < q.level);
 #pragma unroll
-                for (int c = 0; c < 8; ++c)
-                {
-                    if (!(mask >> c & 1u))
-                        continue;
-                    if (next + out < bp.node_cap)
-                    {
-                        bp.stage_nodes[out] = tag | (gx + (c & 1)) | ((gy + (c >> 1 & 1)) << sh) |
-                                              ((gz + (c >> 2 & 1)) << (2 * sh));
-                        bp.stage_skip[out] = produce_me ? ws.cskip[lane][c] : 0u;
-                    }
-                    else
-                        atomicOr(&ctr->overflow, 1ull);
-                    ++out;
+                    for (int c = 0; c < 8; ++c)
+                        bp.child_skip[pi * 8 + c] = produce_me ? ws.cskip[lane][c] : 0u;
                 }
             }
             __syncwarp();
         }
         grid.sync();
-        // the children into the pool, grouped by request (order inside a
-        // request: warp chunks as they were appended)
-        const int64_t nc = level_entries(bp, li + 1, next);
-        unsigned long long* rc = bp.req_count + static_cast<int64_t>(li + 1) * bp.nreq;
-        unsigned long long* cur = bp.req_cursor + static_cast<int64_t>(li + 1) * bp.nreq;
-        if (blockIdx.x == 0 && threadIdx.x < 32)
+        // Phase B: the refined children of level li, in parent order (like
+        // the plain path's compaction), so that neighbouring cells stay
+        // neighbours in the list and their integral-image reads hit L1/L2.
+        // Each block owns a contiguous range of parents.
+        const int64_t per_block = (n + gridDim.x - 1) / gridDim.x;
+        const int64_t lo = static_cast<int64_t>(blockIdx.x) * per_block;
+        const int64_t hi = lo + per_block < n ? lo + per_block : n;
         {
-            unsigned long long carry = static_cast<unsigned long long>(next);
-            for (int r0 = 0; r0 < bp.nreq; r0 += 32)
-            {
-                const int r = r0 + lane;
-                const unsigned long long v = r < bp.nreq ? rc[r] : 0ull;
-                const unsigned long long inc = warp_inclusive_scan(v);
-                if (r < bp.nreq)
-                    cur[r] = carry + inc - v;
-                carry += __shfl_sync(0xffffffffu, inc, 31);
-            }
+            unsigned long long c = 0;
+            for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+                c += __popc(bp.child_masks[i]);
+            unsigned long long tot;
+            block_exclusive_scan(c, &tot);
+            if (threadIdx.x == 0)
+                bp.block_sums[blockIdx.x] = tot;
         }
         grid.sync();
-        const int64_t warp_id = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-        for (int64_t b0 = warp_id * 32; b0 < nc; b0 += nwarps * 32)
         {
-            const int64_t i = b0 + lane;
-            const bool ok = i < nc;
-            const int64_t nd = ok ? bp.stage_nodes[i] : 0;
-            const uint32_t sk = ok ? bp.stage_skip[i] : 0u;
-            const int rq = ok ? static_cast<int>(nd >> kTagShift) : -1;
-            const unsigned grp = __match_any_sync(0xffffffffu, rq);
-            const int leader = __ffs(grp) - 1;
-            unsigned long long pos = 0;
-            if (ok && lane == leader)
-                pos = atomicAdd(&cur[rq], static_cast<unsigned long long>(__popc(grp)));
-            pos = __shfl_sync(0xffffffffu, pos, leader) + __popc(grp & ((1u << lane) - 1u));
-            if (ok)
+            unsigned long long c = 0;
+            for (int64_t b = threadIdx.x; b < static_cast<int64_t>(blockIdx.x); b += blockDim.x)
+                c += bp.block_sums[b];
+            unsigned long long prefix;
+            block_exclusive_scan(c, &prefix);
+            if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
+                ctr->count[li + 1] = static_cast<int64_t>(prefix + bp.block_sums[blockIdx.x]);
+            int64_t carry = next + static_cast<int64_t>(prefix);
+            const int64_t m = (int64_t{ 1 } << li) - 1;
+            const int sh = li + 1;
+            for (int64_t c0 = lo; c0 < hi; c0 += blockDim.x)
             {
-                // children dropped by an overflow still count in the cursors
-                if (pos < static_cast<unsigned long long>(bp.node_cap))
+                const int64_t i = c0 + threadIdx.x;
+                const uint32_t mask = i < hi ? bp.child_masks[i] : 0u;
+                unsigned long long tot;
+                const int64_t out0 = carry + static_cast<int64_t>(block_exclusive_scan(
+                                                     static_cast<unsigned long long>(__popc(mask)), &tot));
+                carry += static_cast<int64_t>(tot);
+                if (!mask)
+                    continue;
+                const int64_t node = bp.nodes[start + i];
+                const int64_t cell = node & kCellMask;
+                const int64_t gx = 2 * (cell & m), gy = 2 * ((cell >> li) & m), gz = 2 * (cell >> (2 * li));
+                const int64_t tag = node & ~kCellMask;
+                int64_t out = out0;
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
                 {
-                    bp.nodes[pos] = nd;
-                    bp.node_skip[pos] = sk;
+                    if (!(mask >> c & 1u))
+                        continue;
+                    if (out < bp.node_cap)
+                    {
+                        bp.nodes[out] = tag | (gx + (c & 1)) | ((gy + (c >> 1 & 1)) << sh) | ((gz + (c >> 2 & 1)) << (2 * sh));
+                        bp.node_skip[out] = i < bp.skip_cap ? bp.child_skip[i * 8 + c] : 0u;
+                    }
+                    else
+                        atomicOr(&ctr->overflow, 1ull);
+                    ++out;
                 }
-                else
-                    atomicOr(&ctr->overflow, 1ull);
             }
         }
         grid.sync();
@@ -318,7 +296,6 @@ __global__ void __launch_bounds__(256) batch_mark_kernel(BatchPlan bp)
 void launch_batch_init(const BatchPlan& bp, cudaStream_t s)
 {
     TH_CUDA(cudaMemsetAsync(bp.ctr, 0, sizeof(BatchCounters), s));
-    TH_CUDA(cudaMemsetAsync(bp.req_count, 0, sizeof(unsigned long long) * (kMaxLevel + 2) * bp.nreq, s));
     batch_init_kernel<<<1, 256, 0, s>>>(bp);
     TH_LAUNCH_CHECK();
 }

@@ -268,7 +268,7 @@ namespace
 // carve, the request table, and the streams the per-request stages run on.
 struct BatchState
 {
-    DevBuf reqs, nodes, node_skip, ctr, stage_nodes, stage_skip, req_work;
+    DevBuf reqs, nodes, node_skip, ctr, child_masks, child_skip, block_sums;
     BatchReq* host_reqs = nullptr; // pinned
     int32_t host_reqs_cap = 0;
     BatchCounters* host_ctr = nullptr; // pinned
@@ -279,7 +279,7 @@ struct BatchState
 
     void release()
     {
-        for (DevBuf* b : { &reqs, &nodes, &node_skip, &ctr, &stage_nodes, &stage_skip, &req_work })
+        for (DevBuf* b : { &reqs, &nodes, &node_skip, &ctr, &child_masks, &child_skip, &block_sums })
             b->release();
         if (host_reqs)
             cudaFreeHost(host_reqs);
@@ -824,9 +824,11 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
         bs.reqs.ensure(sizeof(BatchReq) * n);
         bs.nodes.ensure(sizeof(int64_t) * bs.node_cap);
         bs.node_skip.ensure(sizeof(uint32_t) * bs.node_cap);
-        bs.stage_nodes.ensure(sizeof(int64_t) * bs.node_cap);
-        bs.stage_skip.ensure(sizeof(uint32_t) * bs.node_cap);
-        bs.req_work.ensure(sizeof(unsigned long long) * 2 * (kMaxLevel + 2) * n);
+        // view-skip masks for up to a quarter of the pool's cells in one level
+        const int64_t skip_cap = std::max<int64_t>(bs.node_cap / 4, 1);
+        bs.child_masks.ensure(static_cast<size_t>(bs.node_cap));
+        bs.child_skip.ensure(sizeof(uint32_t) * 8 * skip_cap);
+        bs.block_sums.ensure(sizeof(unsigned long long) * 8 * sm_count());
         bs.ctr.ensure(sizeof(BatchCounters));
         for (int32_t r = 0; r < n; ++r)
         {
@@ -874,10 +876,10 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
         bp.node_skip = bs.node_skip.as<uint32_t>();
         bp.node_cap = bs.node_cap;
         bp.ctr = bs.ctr.as<BatchCounters>();
-        bp.stage_nodes = bs.stage_nodes.as<int64_t>();
-        bp.stage_skip = bs.stage_skip.as<uint32_t>();
-        bp.req_count = bs.req_work.as<unsigned long long>();
-        bp.req_cursor = bp.req_count + (kMaxLevel + 2) * n;
+        bp.child_masks = bs.child_masks.as<uint8_t>();
+        bp.child_skip = bs.child_skip.as<uint32_t>();
+        bp.skip_cap = skip_cap;
+        bp.block_sums = bs.block_sums.as<unsigned long long>();
         bp.variant = -1;
         for (int32_t r = 0; r < n; ++r)
         {

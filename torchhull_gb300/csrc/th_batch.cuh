@@ -49,13 +49,12 @@ struct BatchPlan
     BatchCounters* ctr;
     // (partial << 1) | opengl when every request shares it, -1 otherwise
     int32_t variant;
-    // Children of the level being carved land here unordered, then move to
-    // the pool grouped by request (request-major level lists keep one
-    // request's integral images hot in L2 at a time).
-    int64_t* stage_nodes;   // [node_cap]
-    uint32_t* stage_skip;   // [node_cap]
-    unsigned long long* req_count;  // [(kMaxLevel + 2) * nreq] children per level and request (zeroed)
-    unsigned long long* req_cursor; // [(kMaxLevel + 2) * nreq] next pool position per level and request
+    // per cell of the level being carved: refined children, and the
+    // children's view-skip masks for the first skip_cap cells
+    uint8_t* child_masks;  // [node_cap]
+    uint32_t* child_skip;  // [skip_cap * 8]
+    int64_t skip_cap;
+    unsigned long long* block_sums; // [grid size] children per block
 };
 
 void launch_batch_init(const BatchPlan& bp, cudaStream_t s);
