@@ -624,7 +624,7 @@ def main() -> None:
     ap.add_argument("--carve-kernel", choices=["auto", "views", "items"], default="auto",
                     help="carve kernel: autotuned (default) or forced")
     ap.add_argument("--hetero-count", type=int, default=64)
-    ap.add_argument("--batch-route", choices=["on", "off"], default="on",
+    ap.add_argument("--batch-route", choices=["on", "off"], default="off",
                     help="batched form: requests that fill the GPU alone through the per-request pipeline")
     ap.add_argument("--mc-sizes", default="100,200,300,400,500,600", help="--mode mc: volume sizes")
     ap.add_argument("--rate", type=float, default=200.0)

@@ -298,10 +298,10 @@ typedef enum th_option
      * request shape (sizes, level, modes, dtype, pools); 0: launches them
      * one by one.  Profiled and autotuning runs always launch directly. */
     TH_OPTION_GRAPHS = 2,
-    /* 1 (default): th_visual_hull_batch runs requests that fill the GPU alone
-     * (level >= 8 and at least 16 M mask pixels) through the per-request
-     * pipeline and the others through the shared persistent carve; 0: every
-     * request through the shared carve.  Results are identical. */
+    /* 1: th_visual_hull_batch runs requests that fill the GPU alone (level >= 8
+     * and at least 16 M mask pixels) through the per-request pipeline and the
+     * others through the shared persistent carve; 0 (default): every request
+     * through the shared carve.  Results are identical. */
     TH_OPTION_BATCH_ROUTE = 3
 } th_option;
 th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value);

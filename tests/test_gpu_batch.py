@@ -62,7 +62,7 @@ def test_level9_batch_matches_plain(th, cuda):
 @pytest.mark.parametrize("route", [True, False])
 def test_gpu_filling_requests_routed_or_shared(th, cuda, route):
     # level 8 with 16 views of 1024^2 fills the GPU alone: routed through the
-    # per-request pipeline by default, through the shared carve when routing is off
+    # per-request pipeline when routing is on, through the shared carve when off
     reqs = [scenes.make_request(540, 16, 1024, 8, False, device=cuda),
             scenes.make_request(541, 6, 128, 5, True, device=cuda),
             scenes.make_request(542, 16, 1024, 8, True, device=cuda)]
@@ -74,4 +74,4 @@ def test_gpu_filling_requests_routed_or_shared(th, cuda, route):
             for (v, f), (ev, ef) in zip(got, expected, strict=True):
                 assert torch.equal(v.cpu(), ev) and torch.equal(f.cpu(), ef)
     finally:
-        th._C.set_batch_route(0, True)
+        th._C.set_batch_route(0, False)

@@ -350,7 +350,7 @@ struct th_context
     th_stage_times times{};
     int carve_mode = 0; // TH_OPTION_CARVE_KERNEL
     bool graphs = true;  // TH_OPTION_GRAPHS
-    bool batch_route = true; // TH_OPTION_BATCH_ROUTE
+    bool batch_route = false; // TH_OPTION_BATCH_ROUTE
     std::map<th::TuneKey, th::CarveVariants> carve_tuned;
     cudaEvent_t tune_ev[2] = { nullptr, nullptr };
 };
@@ -958,11 +958,12 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
     }
 }
 
-// A request whose octree alone fills the GPU (level >= 8 and at least 16 M
-// mask pixels) gains nothing from sharing launches and runs through the
-// per-request pipeline (graph replay, autotuned carve kernels; the
-// persistent carve was 6-27 % slower on such requests); the others share the
-// persistent carve.  Results are identical either way.
+// With routing on, a request whose octree alone fills the GPU (level >= 8
+// and at least 16 M mask pixels) runs through the per-request pipeline (graph
+// replay, autotuned carve kernels) and the others share the persistent carve.
+// Off by default: on a batch of four such requests routing gained 2 %, on a
+// mixed batch it lost 16 % (the routed requests no longer overlap the
+// others).  Results are identical either way.
 bool fills_gpu(const th_hull_args& a)
 {
     return a.level >= 8 && a.batch * a.height * a.width >= (int64_t{ 1 } << 24);

@@ -648,7 +648,7 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
     m.def("set_carve_kernel", &set_carve_kernel, "device"_a, "mode"_a,
           "Carve kernel choice: 0 autotune, 1 views over lanes, 2 (parent, view) items.");
     m.def("set_batch_route", &set_batch_route, "device"_a, "enable"_a,
-          "Batched form: run requests that fill the GPU alone through the per-request pipeline (default on).");
+          "Batched form: run requests that fill the GPU alone through the per-request pipeline (default off).");
     m.def("set_graphs", &set_graphs, "device"_a, "enable"_a,
           "Replay each request shape's pipeline as a captured CUDA graph (default on).");
     pybind11::class_<HullContext>(m, "HullContext", "Context with its own device pools (one request at a time).")
