@@ -17,9 +17,12 @@ carve launch over the Q octrees).  Beside it: the plain drop-in
 (torchhull_gb300.visual_hull, one request per call) as hulls/s and p50/p99
 per hull, stage times from CUDA events the library records between stages on
 the request's stream (the largest stage is the roofline line), and `e2e`: the
-batched step with the masks copied in from pinned host memory and the meshes
-copied back inside the timed region.  Under torchrun every rank serves its own
-requests (weak scaling, no collective on the data path).
+plain drop-in fed from pinned host memory, every request's masks and
+transforms copied in and its mesh copied back inside the timed region, the
+copies overlapped with the neighbouring hulls on two side streams
+(`e2e_batched`: the batched step with the same copies, not overlapped).
+Under torchrun every rank serves its own requests (weak scaling, no
+collective on the data path).
 
 --mode hetero: 64 heterogeneous requests (views U{4..48}, side
 U{256,512,768,1024}, level U{6..9}, partial ~ Bernoulli(0.3)), batched vs plain.
@@ -220,6 +223,72 @@ def timed_plain(th, reqs, steps: int, dev, world: int, local: int, profile: bool
     return max_over_ranks(start.elapsed_time(stop), world, dev), sorted(per_hull), stages
 
 
+def e2e_plain_pipelined(th, reqs, steps: int, dev, world: int) -> tuple[float, int, int]:
+    """End to end through the plain drop-in (torchhull_gb300.visual_hull) from
+    pinned host memory: hull i runs on the compute stream while request i+1's
+    masks and transforms are copied in on a second stream (two device slots)
+    and hull i-1's mesh is copied out to pinned host memory on a third.  Every
+    copy of every step is inside the timed region.  Returns (hulls/s, h2d bytes
+    per step, d2h bytes per step)."""
+    import torch
+    import torch.distributed as dist
+
+    Q = len(reqs)
+    shape, tshape = reqs[0].masks.shape, reqs[0].transforms.shape
+    assert all(r.masks.shape == shape and r.transforms.shape == tshape for r in reqs)
+    host_in = [(r.masks.cpu().pin_memory(), r.transforms.cpu().pin_memory()) for r in reqs]
+    slots = [(torch.empty_like(reqs[0].masks), torch.empty_like(reqs[0].transforms)) for _ in range(2)]
+    # the meshes are deterministic: pinned result buffers sized from one untimed call each
+    host_out = []
+    for r in reqs:
+        v, f = th.visual_hull(**r.kwargs())
+        host_out.append((torch.empty(v.shape, dtype=v.dtype, pin_memory=True),
+                         torch.empty(f.shape, dtype=f.dtype, pin_memory=True)))
+    h2d = sum(m.numel() * m.element_size() + t.numel() * t.element_size() for m, t in host_in)
+    d2h = sum(v.numel() * v.element_size() + f.numel() * f.element_size() for v, f in host_out)
+
+    comp = torch.cuda.current_stream(dev)
+    cin = torch.cuda.Stream(dev)
+    cout = torch.cuda.Stream(dev)
+    ready = [torch.cuda.Event() for _ in range(2)]
+    free = [torch.cuda.Event() for _ in range(2)]
+    order = [q for _ in range(steps) for q in range(Q)]
+
+    def copy_in(i):
+        s = i % 2
+        with torch.cuda.stream(cin):
+            cin.wait_event(free[s])  # hull i-2 is done with slot s
+            slots[s][0].copy_(host_in[order[i]][0], non_blocking=True)
+            slots[s][1].copy_(host_in[order[i]][1], non_blocking=True)
+            ready[s].record(cin)
+
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    copy_in(0)
+    for i, q in enumerate(order):
+        if i + 1 < len(order):
+            copy_in(i + 1)
+        s = i % 2
+        comp.wait_event(ready[s])
+        kw = reqs[q].kwargs()
+        kw["masks"], kw["transforms"] = slots[s]
+        v, f = th.visual_hull(**kw)
+        free[s].record(comp)
+        done = torch.cuda.Event()
+        done.record(comp)
+        with torch.cuda.stream(cout):
+            cout.wait_event(done)
+            host_out[q][0].copy_(v, non_blocking=True)
+            host_out[q][1].copy_(f, non_blocking=True)
+            v.record_stream(cout)
+            f.record_stream(cout)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    return Q * steps * world / e2e_s, h2d, d2h
+
+
 def run_gb300(args) -> dict | None:
     import torch
     import torch.distributed as dist
@@ -234,6 +303,7 @@ def run_gb300(args) -> dict | None:
         dist.init_process_group("nccl", device_id=dev)
     th._C.set_carve_kernel(local, {"auto": 0, "views": 1, "items": 2}[args.carve_kernel])
     th._C.set_batch_route(local, args.batch_route == "on")
+    th._C.set_field_ones(local, args.field_ones == "on")
 
     if args.mode == "hetero":
         return finish(run_hetero(args, th, scenes, dev, world, rank), world)
@@ -267,18 +337,18 @@ def run_gb300(args) -> dict | None:
     plain_ms, per_hull, stages = timed_plain(th, reqs, args.steps, dev, world, local, profile=True)
     plain_value = Q * args.steps * world / (plain_ms / 1000.0)
 
-    # end to end: batched step with masks copied in from pinned host memory and meshes copied back
+    # end to end through the plain drop-in, copies pipelined against the hulls
+    e2e_steps = max(1, args.steps // 2)
+    e2e_value, h2d, d2h = e2e_plain_pipelined(th, reqs, e2e_steps, dev, world)
+
+    # end to end through the batched form: copies in, one batch call, meshes out, per step
     host_masks = [r.masks.cpu().pin_memory() for r in reqs]
     host_tf = [r.transforms.cpu().pin_memory() for r in reqs]
     dev_masks = [torch.empty_like(r.masks) for r in reqs]
     dev_tf = [torch.empty_like(r.transforms) for r in reqs]
-    h2d = sum(m.numel() * m.element_size() for m in host_masks) + sum(x.numel() * x.element_size() for x in host_tf)
-    # the meshes are deterministic: pinned result buffers sized from one untimed call
     first = th._C.visual_hull_batch(tuples)
     host_out = [(torch.empty(v.shape, dtype=v.dtype, pin_memory=True),
                  torch.empty(f.shape, dtype=f.dtype, pin_memory=True)) for v, f in first]
-    d2h = sum(vh.numel() * vh.element_size() + fh.numel() * fh.element_size() for vh, fh in host_out)
-    e2e_steps = max(1, args.steps // 2)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -292,8 +362,7 @@ def run_gb300(args) -> dict | None:
             vh.copy_(v, non_blocking=True)
             fh.copy_(f, non_blocking=True)
         torch.cuda.synchronize()
-    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
-    e2e_value = Q * e2e_steps * world / e2e_s
+    e2e_batched = Q * e2e_steps * world / max_over_ranks(time.perf_counter() - t0, world, dev)
 
     if rank != 0:
         return finish(None, world)
@@ -334,6 +403,7 @@ def run_gb300(args) -> dict | None:
         "config": {"workload": WORKLOAD, "requests_per_step": Q, "level": LEVEL, "views": VIEWS, "side": SIDE,
                    "l2": "inputs larger than L2 (128 MiB of masks + 128 MiB SAT per request)",
                    "path": "batched form (th_visual_hull_batch: one persistent carve launch per step)",
+                   "field_ones": args.field_ones,
                    "mesh_verts": nv, "mesh_faces": nf, "leaves": levels[-1], "corners": corners},
         "plain": {"value": plain_value, "unit": "hulls/s", "p50_ms": percentile(per_hull, 50),
                   "p99_ms": percentile(per_hull, 99), "path": "torchhull_gb300.visual_hull, one request per call"},
@@ -342,7 +412,11 @@ def run_gb300(args) -> dict | None:
         "p99_ms": percentile(per_hull, 99),
         "stage_ms": mean,
         "e2e": {"value": e2e_value, "unit": "hulls/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h,
+                "path": "torchhull_gb300.visual_hull from pinned host memory, copies in/out pipelined on "
+                        "two side streams against the hulls"},
+        "e2e_batched": {"value": e2e_batched, "unit": "hulls/s",
+                        "path": "th_visual_hull_batch per step, copies in, batch, meshes out, not overlapped"},
         "roofline": {"bound": "hbm", "kernel": dom[1], "stage": dom[0], "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes": dom[3], "ms": dom[2], "traffic": None},
@@ -626,6 +700,8 @@ def main() -> None:
     ap.add_argument("--hetero-count", type=int, default=64)
     ap.add_argument("--batch-route", choices=["on", "off"], default="off",
                     help="batched form: requests that fill the GPU alone through the per-request pipeline")
+    ap.add_argument("--field-ones", choices=["on", "off"], default="on",
+                    help="field: test a bitmap of all-ones 2x2 pixel footprints before sampling the masks")
     ap.add_argument("--mc-sizes", default="100,200,300,400,500,600", help="--mode mc: volume sizes")
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--duration", type=float, default=10.0)

@@ -302,7 +302,13 @@ typedef enum th_option
      * and at least 16 M mask pixels) through the per-request pipeline and the
      * others through the shared persistent carve; 0 (default): every request
      * through the shared carve.  Results are identical. */
-    TH_OPTION_BATCH_ROUTE = 3
+    TH_OPTION_BATCH_ROUTE = 3,
+    /* 1 (default): the field stage first builds a bitmap of the 2x2 pixel
+     * footprints whose four mask values are exactly 1 and returns the factor
+     * 1 for a sample there without reading the masks (a bilinear sample of
+     * four ones is exactly 1); 0: every sample reads its four pixels.
+     * Results are identical. */
+    TH_OPTION_FIELD_ONES = 4
 } th_option;
 th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value);
 th_status th_context_stage_times(const th_context* ctx, th_stage_times* out);

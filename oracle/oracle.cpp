@@ -791,6 +791,20 @@ int oracle_integral_image(const void* masks, int masks_dtype, int64_t B, int64_t
     return 0;
 }
 
+int64_t oracle_bilerp_ones_failures(uint32_t lo_bits, uint32_t hi_bits)
+{
+    int64_t bad = 0;
+    for (uint64_t u = lo_bits; u <= hi_bits; ++u)
+    {
+        float t;
+        const uint32_t b = static_cast<uint32_t>(u);
+        std::memcpy(&t, &b, sizeof(float));
+        if (bilerp(1.f, 1.f, 1.f, 1.f, t, t) != 1.f)
+            ++bad;
+    }
+    return bad;
+}
+
 } // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -76,6 +76,11 @@ void oracle_hull_free(oracle_hull* h);
 // it (visual_hull_cuda.cu:76-90).  out: [B,H,W] float32.
 int oracle_integral_image(const void* masks, int masks_dtype, int64_t B, int64_t H, int64_t W, float* out, int nthreads);
 
+// Number of float32 weights t, over the bit patterns lo_bits..hi_bits (both
+// of one sign), for which bilerp(1, 1, 1, 1, t, t) is not exactly 1 (the
+// all-ones footprint shortcut of the GPU field relies on 0 for [0, 1.25]).
+int64_t oracle_bilerp_ones_failures(uint32_t lo_bits, uint32_t hi_bits);
+
 // gaussian_blur (gaussian_blur_cuda.cu:73-114 dense, :288-507 sparse).
 // out: [B,H,W,1] of out_dtype.  Returns 0 on success.
 int oracle_gaussian_blur(const void* images,

@@ -71,6 +71,8 @@ def lib() -> ctypes.CDLL:
         L.oracle_mesh_copy.argtypes = [vp, vp, vp]
         L.oracle_mesh_free.argtypes = [vp]
         L.oracle_candidate_wireframe.argtypes = [vp, i64, i32, f32, f32, f32, f32, vp, vp]
+        L.oracle_bilerp_ones_failures.restype = i64
+        L.oracle_bilerp_ones_failures.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
         _lib = L
     return _lib
 

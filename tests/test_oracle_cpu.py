@@ -194,3 +194,15 @@ def test_thread_count_does_not_change_results(small):
     a = oracle.visual_hull(small.masks, small.transforms, 5, (-1, -1, -1), 2.0, True, "opengl", nthreads=1)
     b = oracle.visual_hull(small.masks, small.transforms, 5, (-1, -1, -1), 2.0, True, "opengl", nthreads=8)
     assert np.array_equal(a.verts, b.verts) and np.array_equal(a.faces, b.faces)
+
+
+def test_bilerp_of_ones_is_exactly_one():
+    """The GPU field returns 1 for a sample whose 2x2 footprint is all ones
+    without interpolating; that needs bilerp(1, 1, 1, 1, t, t) == 1 for every
+    float32 weight in [0, 1] (checked over [0, 1.25], every value).  Negative
+    weights are excluded by the shortcut and do fail."""
+    L = oracle.lib()
+    one_and_a_quarter = int(np.array(1.25, np.float32).view(np.uint32))
+    assert L.oracle_bilerp_ones_failures(0, one_and_a_quarter) == 0
+    minus = int(np.array(-(2.0**-25) * (1 + 2.0**-23), np.float32).view(np.uint32))
+    assert L.oracle_bilerp_ones_failures(minus, minus + 16) > 0

@@ -124,8 +124,8 @@ bool is_image_dtype(int d)
 // Pools and the state of the last request of one context.
 struct HullSlot
 {
-    DevBuf tf, sat, nodes, node_skip, child_masks, child_skip, tile_sums, bitmap, word_rank, rowbits, rows, corners,
-            values, codes, emask, soup_off, vbase, counters, flags;
+    DevBuf tf, sat, ones, nodes, node_skip, child_masks, child_skip, tile_sums, bitmap, word_rank, rowbits, rows,
+            corners, values, codes, emask, soup_off, vbase, counters, flags;
     int64_t node_cap = 0, corner_cap = 0, parent_cap = 0;
     HullPlan plan{};
     DevCounters* host = nullptr; // pinned copy of the counters
@@ -156,7 +156,7 @@ struct HullSlot
 
     std::vector<const DevBuf*> buffers() const
     {
-        return { &tf,     &sat,  &nodes,    &node_skip, &child_masks, &child_skip, &tile_sums,
+        return { &tf,     &sat,  &ones,     &nodes,     &node_skip,   &child_masks, &child_skip, &tile_sums,
                  &bitmap, &word_rank, &rowbits, &rows, &corners,    &values,     &codes,
                  &emask,  &soup_off, &vbase,   &counters, &flags, &rq };
     }
@@ -351,6 +351,7 @@ struct th_context
     int carve_mode = 0; // TH_OPTION_CARVE_KERNEL
     bool graphs = true;  // TH_OPTION_GRAPHS
     bool batch_route = false; // TH_OPTION_BATCH_ROUTE
+    bool field_ones = true;   // TH_OPTION_FIELD_ONES
     std::map<th::TuneKey, th::CarveVariants> carve_tuned;
     cudaEvent_t tune_ev[2] = { nullptr, nullptr };
 };
@@ -424,7 +425,7 @@ int64_t max_nodes(int level)
 // Sizes the pools of slot s for request a and fills its plan.
 // batch_slot: the request is part of a batch, whose octree lives in the
 // batch's shared node pool, so the slot keeps no octree pools of its own.
-void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool batch_slot = false)
+void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_ones, bool batch_slot = false)
 {
     const int L = a->level;
     const int64_t B = a->batch, H = a->height, W = a->width;
@@ -452,6 +453,9 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool batch_slo
 
     s.tf.ensure(sizeof(float) * std::max<int64_t>(B, 1) * 16);
     s.sat.ensure(sizeof(float) * std::max<int64_t>(B * H * W, 1));
+    const int64_t WW = (W + 31) / 32;
+    if (field_ones)
+        s.ones.ensure(sizeof(uint32_t) * std::max<int64_t>(B * H * WW, 1));
     s.nodes.ensure(sizeof(int64_t) * node_cap);
     s.node_skip.ensure(sizeof(uint32_t) * node_cap);
     s.child_masks.ensure(node_cap);
@@ -507,6 +511,9 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool batch_slo
     p.nonbinary = s.flags.as<unsigned int>();
     // exact integer box sums need every SAT sum of two entries below 2^24
     p.skip_ok = B > 0 && H > 0 && W > 0 && H * W <= (int64_t{ 1 } << 23);
+    p.field_ones = field_ones && B > 0 && H > 0 && W > 0;
+    p.ones = field_ones ? s.ones.as<uint32_t>() : nullptr;
+    p.WW = WW;
     p.R = R;
     p.WR = WR;
     p.bitmap = s.bitmap.as<uint64_t>();
@@ -669,7 +676,7 @@ void run_hull_once(th_context* ctx,
     const int L = a->level;
     for (int attempt = 0; attempt < 8; ++attempt)
     {
-        prepare(s, a, st);
+        prepare(s, a, st, ctx->field_ones);
         for (int i = 0; i < kMaxLevel; ++i)
             s.plan.carve_variant[i] = variants[i];
         const HullPlan& p = s.plan;
@@ -834,7 +841,7 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
         {
             const th_hull_args* a = &args[r];
             HullSlot& s = ctx->batch[r];
-            prepare(s, a, st, true);
+            prepare(s, a, st, ctx->field_ones, true);
             if (attempt == 0)
             {
                 launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), st);
@@ -1298,6 +1305,8 @@ th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value)
             ctx->graphs = value != 0;
         else if (option == TH_OPTION_BATCH_ROUTE && (value == 0 || value == 1))
             ctx->batch_route = value != 0;
+        else if (option == TH_OPTION_FIELD_ONES && (value == 0 || value == 1))
+            ctx->field_ones = value != 0;
         else
             throw ArgError{ TH_ERR_INVALID_ARGUMENT, "unknown option or value" };
     });

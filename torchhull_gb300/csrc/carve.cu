@@ -62,7 +62,10 @@ namespace th
 namespace
 {
 
-constexpr int kWarps = 8; // warps per block of the classify kernels
+#ifndef TH_CARVE_WARPS
+#define TH_CARVE_WARPS 8
+#endif
+constexpr int kWarps = TH_CARVE_WARPS; // warps per block of the classify kernels
 #ifndef TH_CARVE_MIN_BLOCKS
 #define TH_CARVE_MIN_BLOCKS 2
 #endif

@@ -198,11 +198,10 @@ __device__ __forceinline__ float mask_sample(const HullPlan& p, const void* mask
 // are padding, for which the interpolation gives the same result (0, 1 or
 // NaN) for either weight.
 template <int DT, bool PARTIAL>
-__device__ __forceinline__ float view_factor(const HullPlan& p, const void* masks, int64_t b, float wx, float wy, float wz, float Hf, float Wf)
+__device__ __forceinline__ float view_factor(const HullPlan& p, const void* masks, int64_t b, const float4 (&rows)[3], float wx, float wy, float wz, float Hf, float Wf)
 {
-    const float* m = p.tf + 16 * b;
     float px, py;
-    to_pixel(m, wx, wy, wz, p.opengl, Hf, Wf, px, py);
+    to_pixel_rows(rows[0], rows[1], rows[2], wx, wy, wz, p.opengl, Hf, Wf, px, py);
     const float pad = PARTIAL ? 1.f : 0.f;
     // 1 <= round(q) < size - 1 (half away from zero) exactly when 0.5 <= q < size - 1.5
     if (PARTIAL && !(px >= 0.5f && px < __fsub_rn(Wf, 1.5f) && py >= 0.5f && py < __fsub_rn(Hf, 1.5f)))
@@ -219,6 +218,17 @@ __device__ __forceinline__ float view_factor(const HullPlan& p, const void* mask
         rx.f = __int2float_rn(rx.i);
     }
     const int64_t y0 = ry.i, x0 = rx.i;
+    // All-ones footprint: the sample is exactly 1.  The weights q - round(q
+    // - 0.5) lie in [0, 1] whenever the footprint starts inside the image
+    // (q - 0.5 is exact for q >= 0.5; below, a start of 0 means q in (0,
+    // 0.5)), except for q = NaN, whose sample is NaN.
+    if (p.field_ones && static_cast<uint64_t>(y0) < static_cast<uint64_t>(p.H) &&
+        static_cast<uint64_t>(x0) < static_cast<uint64_t>(p.W) && px == px && py == py)
+    {
+        const uint32_t word = __ldg(p.ones + (b * p.H + y0) * p.WW + (x0 >> 5));
+        if ((word >> (x0 & 31)) & 1u)
+            return 1.f;
+    }
     float v00, v10, v01, v11;
     if (PARTIAL)
     {
@@ -241,6 +251,41 @@ __device__ __forceinline__ float view_factor(const HullPlan& p, const void* mask
     return bilerp(v00, v10, v01, v11, ty, tx);
 }
 
+// The all-ones footprint bitmap of the masks (HullPlan::ones): one warp per
+// mask row y, 32 columns per step; a lane tests its column in rows y and y+1
+// and takes its right neighbour's result by a shuffle (the last lane loads
+// the column after the step).  Columns x = W-1 and rows y = H-1 have no 2x2
+// footprint and get 0.
+template <int DT>
+__global__ void __launch_bounds__(256) ones_kernel(HullPlan p)
+{
+    const void* masks = p.rq->masks;
+    const int64_t H = p.H, W = p.W, rows = p.B * H;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t row = warp; row < rows; row += nwarps)
+    {
+        const int64_t y = row % H;
+        const bool below = y + 1 < H;
+        const int64_t base = row * W;
+        for (int64_t x0 = 0; x0 < W; x0 += 32)
+        {
+            const int64_t x = x0 + lane;
+            bool col = false; // column x is 1 in rows y and y+1
+            if (x < W && below)
+                col = load_f32<DT>(masks, base + x) == 1.f && load_f32<DT>(masks, base + W + x) == 1.f;
+            bool next = __shfl_down_sync(0xffffffffu, col, 1);
+            if (lane == 31)
+                next = x + 1 < W && below && load_f32<DT>(masks, base + x + 1) == 1.f &&
+                       load_f32<DT>(masks, base + W + x + 1) == 1.f;
+            const uint32_t word = __ballot_sync(0xffffffffu, col && next);
+            if (lane == 0)
+                p.ones[row * p.WW + (x0 >> 5)] = word;
+        }
+    }
+}
+
 // accumulate_hull_counts_{full,partial} (visual_hull_cuda.cu:419-520): the
 // views [b0, b1) multiplied into each corner's running product in ascending
 // view order (b0 == 0 starts it at 1).  Views go in chunks of kFieldViews, one
@@ -251,6 +296,17 @@ constexpr int64_t kFieldViews = 16;
 template <int DT, bool PARTIAL>
 __global__ void __launch_bounds__(256) field_kernel(HullPlan p, int64_t b0, int64_t b1)
 {
+    // the projection rows of the chunk's views, read from shared memory by
+    // every (corner, view) pair instead of twelve global loads each
+    __shared__ float4 rows[kFieldViews][3];
+    const int nv = static_cast<int>(b1 - b0);
+    for (int i = threadIdx.x; i < 3 * nv; i += blockDim.x)
+    {
+        const int v = i / 3, r = i - 3 * (i / 3);
+        const int row = r < 2 ? r : (p.opengl ? 3 : 2);
+        rows[v][r] = *reinterpret_cast<const float4*>(p.tf + 16 * (b0 + v) + 4 * row);
+    }
+    __syncthreads();
     const int64_t n = p.ctr->corners;
     const int64_t R = p.R;
     const float inv_rc = __fdiv_rn(1.f, static_cast<float>(R - 1)); // exact: a power of two
@@ -270,8 +326,8 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p, int64_t b0, int6
         const float wz = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gz)), inv_rc), length, cz);
         float value = b0 == 0 ? 1.f : p.values[t];
 #pragma unroll 4
-        for (int64_t b = b0; b < b1; ++b)
-            value = __fmul_rn(value, view_factor<DT, PARTIAL>(p, masks, b, wx, wy, wz, Hf, Wf));
+        for (int v = 0; v < nv; ++v)
+            value = __fmul_rn(value, view_factor<DT, PARTIAL>(p, masks, b0 + v, rows[v], wx, wy, wz, Hf, Wf));
         p.values[t] = value;
     }
 }
@@ -534,6 +590,15 @@ void launch_rank_corners(const HullPlan& p, cudaStream_t s)
 
 void launch_field(const HullPlan& p, cudaStream_t s)
 {
+    if (p.field_ones)
+    {
+        bool ok = dispatch_image_dtype(p.masks_dtype, [&]<int DT>() {
+            ones_kernel<DT><<<grid_for(p.B * p.H * 32, 256), 256, 0, s>>>(p);
+        });
+        if (!ok)
+            throw CudaError{ cudaErrorInvalidValue, "hull field: unsupported mask dtype" };
+        TH_LAUNCH_CHECK();
+    }
     const int grid = grid_for(p.corner_cap, 256);
     // at least one launch, so that B == 0 still writes the empty product 1
     for (int64_t b0 = 0; b0 == 0 || b0 < p.B; b0 += kFieldViews)

@@ -216,31 +216,27 @@ __device__ __forceinline__ uint32_t fast_div(const FastDiv& f, uint32_t n)
     return (t + ((n - t) >> f.s1)) >> f.s2;
 }
 
-// K*T*[x,y,z,1] with nested fmaf (visual_hull_cuda.cu:142-156). m is row-major 4x4.
-__device__ __forceinline__ float project_row(const float* m, float x, float y, float z)
+// Pixel position of a camera-space point (image_utils.h:62-82) from the
+// view's rows x, y and divisor (w for OpenGL, z for OpenCV) of its row-major
+// 4x4 matrix: K*T*[x,y,z,1] with nested fmaf (visual_hull_cuda.cu:142-156),
+// then the division and, for OpenGL, (n + 1) * size / 2 - 0.5 (x / 2 ==
+// x * 0.5 exactly).
+__device__ __forceinline__ void to_pixel_rows(const float4& rx, const float4& ry, const float4& rd, float x, float y, float z, bool opengl, float H, float W, float& px, float& py)
 {
-    return __fmaf_rn(m[0], x, __fmaf_rn(m[1], y, __fmaf_rn(m[2], z, m[3])));
-}
-
-// Pixel position of a camera-space point (image_utils.h:62-82).
-__device__ __forceinline__ void to_pixel(const float* m, float x, float y, float z, bool opengl, float H, float W, float& px, float& py)
-{
-    float cx = project_row(m + 0, x, y, z);
-    float cy = project_row(m + 4, x, y, z);
+    const float cx = __fmaf_rn(rx.x, x, __fmaf_rn(rx.y, y, __fmaf_rn(rx.z, z, rx.w)));
+    const float cy = __fmaf_rn(ry.x, x, __fmaf_rn(ry.y, y, __fmaf_rn(ry.z, z, ry.w)));
+    const float cd = __fmaf_rn(rd.x, x, __fmaf_rn(rd.y, y, __fmaf_rn(rd.z, z, rd.w)));
     if (opengl)
     {
-        float cw = project_row(m + 12, x, y, z);
-        float nx = __fdiv_rn(cx, cw);
-        float ny = __fdiv_rn(cy, cw);
-        // x / 2 == x * 0.5 exactly
+        const float nx = __fdiv_rn(cx, cd);
+        const float ny = __fdiv_rn(cy, cd);
         px = __fsub_rn(__fmul_rn(__fmul_rn(__fadd_rn(nx, 1.f), W), 0.5f), 0.5f);
         py = __fsub_rn(__fmul_rn(__fmul_rn(__fadd_rn(ny, 1.f), H), 0.5f), 0.5f);
     }
     else
     {
-        float cz = project_row(m + 8, x, y, z);
-        px = __fsub_rn(__fdiv_rn(cx, cz), 0.5f);
-        py = __fsub_rn(__fdiv_rn(cy, cz), 0.5f);
+        px = __fsub_rn(__fdiv_rn(cx, cd), 0.5f);
+        py = __fsub_rn(__fdiv_rn(cy, cd), 0.5f);
     }
 }
 

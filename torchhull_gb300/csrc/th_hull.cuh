@@ -73,6 +73,14 @@ struct HullPlan
     uint8_t carve_variant[kMaxLevel];
     const unsigned int* nonbinary; // set by the SAT pass when a mask value is not 0/1
     bool skip_ok;                  // exact integer SAT sums (H * W < 2^24)
+    // All-ones footprints: bit x of word (b*H + y)*WW + x/32 is set when the
+    // mask values of view b at (x, y), (x+1, y), (x, y+1) and (x+1, y+1) are
+    // all exactly 1 (as floats).  A bilinear sample whose footprint is such a
+    // 2x2 block is exactly 1 (lerp(1, 1, t) == 1 for every t in [0, 1.25],
+    // checked exhaustively), so the field skips the four mask reads.
+    bool field_ones;
+    uint32_t* ones; // [B*H*WW]
+    int64_t WW;
     // corner grid: R^3 points, one bit each, rows of WR 64-bit words (x fastest)
     int64_t R, WR;
     uint64_t* bitmap;     // [R*R*WR]

@@ -37,8 +37,9 @@ def estimate_bytes(req: HullRequest) -> int:
     """Device bytes a request holds while it runs: its inputs plus the pools it needs.
 
     Mirrors the pool sizing of the C library (csrc/capi.cu: prepare): SAT,
-    node and corner pools (capped at 16 M entries, the initial capacity) and
-    the corner bitmap with its rank words.
+    node and corner pools (capped at 16 M entries, the initial capacity), the
+    all-ones footprint bitmap of the field and the corner bitmap with its
+    rank words.
     """
     B, H, W = req.masks.shape[:3]
     inputs = req.masks.numel() * req.masks.element_size() + req.transforms.numel() * req.transforms.element_size()
@@ -49,10 +50,11 @@ def estimate_bytes(req: HullRequest) -> int:
     corners = min(R**3, 1 << 24)
     parents = min(_max_nodes(L), 1 << 22)
     sat = 4 * B * H * W
+    ones = 4 * B * H * ((W + 31) // 32)
     node_pool = nodes * (8 + 4 + 1) + parents * 32
     corner_pool = corners * (8 + 4 + 1 + 1 + 4 + 4)
     bitmap = R * R * WR * (8 + 4) + R * R * 4 + (R * R + 31) // 32 * 4
-    return int(inputs + sat + node_pool + corner_pool + bitmap)
+    return int(inputs + sat + ones + node_pool + corner_pool + bitmap)
 
 
 @dataclasses.dataclass
