@@ -21,6 +21,10 @@ CASES = {
     "partial_40": dict(seed=43, views=40, side=160, level=6, partial=True),
     "partial_opencv_20": dict(seed=44, views=20, side=192, level=6, partial=True, convention="opencv"),
     "full_opencv_33": dict(seed=45, views=33, side=128, level=6, partial=False, convention="opencv"),
+    # widths that are no multiple of 32: the bitmap comes from its own kernel,
+    # not from the integral-image pass
+    "partial_150": dict(seed=49, views=14, side=150, level=6, partial=True),
+    "full_97": dict(seed=50, views=9, side=97, level=6, partial=False),
 }
 
 

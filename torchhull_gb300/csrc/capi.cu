@@ -461,7 +461,7 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_one
     s.child_masks.ensure(node_cap);
     s.child_skip.ensure(sizeof(uint32_t) * 8 * parent_cap);
     s.flags.ensure(sizeof(unsigned int) * 4);
-    const int64_t scan_items = std::max({ node_cap, corner_cap, R * R });
+    const int64_t scan_items = std::max({ node_cap, corner_cap, R * R * WR });
     s.tile_sums.ensure(sizeof(unsigned long long) * ((scan_items + kScanTile - 1) / kScanTile + 1));
     const int64_t words = R * R * WR;
     const int64_t rwords = (R * R + 31) / 32;

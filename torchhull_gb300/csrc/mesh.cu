@@ -118,16 +118,17 @@ struct RowEpilogue
     }
 };
 
+// One scan item per bitmap word of the touched rows (item k: word k % WR of
+// row rows[k / WR]), so that a thread emits the corners of a few words, not
+// of several whole rows.
 struct CornerCount
 {
     HullPlan p;
     __device__ unsigned long long operator()(int64_t k) const
     {
-        const int64_t base = static_cast<int64_t>(p.rows[k]) * p.WR;
-        unsigned long long s = 0;
-        for (int64_t w = 0; w < p.WR; ++w)
-            s += __popcll(p.bitmap[base + w]);
-        return s;
+        const uint32_t wr = static_cast<uint32_t>(p.WR), kk = static_cast<uint32_t>(k);
+        const int64_t w = static_cast<int64_t>(p.rows[kk / wr]) * p.WR + (kk % wr);
+        return static_cast<unsigned long long>(__popcll(p.bitmap[w]));
     }
 };
 
@@ -136,26 +137,26 @@ struct CornerEmit
     HullPlan p;
     __device__ void operator()(int64_t k, unsigned long long off, unsigned long long) const
     {
-        const int64_t row = p.rows[k];
-        const int64_t base = row * p.WR;
-        const uint32_t ry = static_cast<uint32_t>(row) % static_cast<uint32_t>(p.R);
-        const uint32_t rz = static_cast<uint32_t>(row) / static_cast<uint32_t>(p.R);
+        const uint32_t wr = static_cast<uint32_t>(p.WR), kk = static_cast<uint32_t>(k);
+        const uint32_t row = p.rows[kk / wr], wi = kk % wr;
+        const int64_t w = static_cast<int64_t>(row) * p.WR + wi;
+        uint64_t word = p.bitmap[w];
+        p.word_rank[w] = static_cast<uint32_t>(off);
+        if (!word)
+            return;
+        const uint32_t ry = row % static_cast<uint32_t>(p.R);
+        const uint32_t rz = row / static_cast<uint32_t>(p.R);
         uint64_t out = off;
-        for (int64_t w = 0; w < p.WR; ++w)
+        while (word)
         {
-            uint64_t word = p.bitmap[base + w];
-            p.word_rank[base + w] = static_cast<uint32_t>(out);
-            while (word)
+            const int bit = __ffsll(static_cast<long long>(word)) - 1;
+            if (static_cast<int64_t>(out) < p.corner_cap)
             {
-                const int bit = __ffsll(static_cast<long long>(word)) - 1;
-                if (static_cast<int64_t>(out) < p.corner_cap)
-                {
-                    p.corners[out] = pack_corner(w * 64 + bit, ry, rz);
-                    p.emask[out] = 0;
-                }
-                ++out;
-                word &= word - 1;
+                p.corners[out] = pack_corner(static_cast<int64_t>(wi) * 64 + bit, ry, rz);
+                p.emask[out] = 0;
             }
+            ++out;
+            word &= word - 1;
         }
     }
 };
@@ -251,37 +252,54 @@ __device__ __forceinline__ float view_factor(const HullPlan& p, const void* mask
     return bilerp(v00, v10, v01, v11, ty, tx);
 }
 
-// The all-ones footprint bitmap of the masks (HullPlan::ones): one warp per
-// mask row y, 32 columns per step; a lane tests its column in rows y and y+1
-// and takes its right neighbour's result by a shuffle (the last lane loads
-// the column after the step).  Columns x = W-1 and rows y = H-1 have no 2x2
-// footprint and get 0.
+// The all-ones footprint bitmap of the masks (HullPlan::ones).  A warp owns
+// 32 columns of a band of kOnesBand rows of one view: it loads the band's
+// rows and the row below at once (the last lane also the column after the
+// chunk), then per row a lane tests its column, takes its right neighbour's
+// result by a shuffle, and a ballot gives the row's "this column and the next
+// are 1" bits; a footprint word is the AND of two consecutive rows' bits.
+// Each mask row is read once, plus one row per band.  Columns x = W-1 and the
+// last row have no 2x2 footprint and get 0.
+constexpr int kOnesBand = 16;
+
 template <int DT>
 __global__ void __launch_bounds__(256) ones_kernel(HullPlan p)
 {
     const void* masks = p.rq->masks;
-    const int64_t H = p.H, W = p.W, rows = p.B * H;
+    const int64_t H = p.H, W = p.W, WW = p.WW;
+    const int64_t bands = (H + kOnesBand - 1) / kOnesBand;
+    const int64_t units = p.B * bands * WW;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-    for (int64_t row = warp; row < rows; row += nwarps)
+    for (int64_t u = warp; u < units; u += nwarps)
     {
-        const int64_t y = row % H;
-        const bool below = y + 1 < H;
-        const int64_t base = row * W;
-        for (int64_t x0 = 0; x0 < W; x0 += 32)
+        // chunk fastest: neighbouring warps read neighbouring segments of a row
+        const int64_t chunk = u % WW, vb = u / WW;
+        const int64_t band = vb % bands, b = vb / bands;
+        const int64_t y0 = band * kOnesBand;
+        const int64_t x = chunk * 32 + lane;
+        const int64_t view = b * H;
+        float own[kOnesBand + 1], right[kOnesBand + 1];
+#pragma unroll
+        for (int i = 0; i <= kOnesBand; ++i)
         {
-            const int64_t x = x0 + lane;
-            bool col = false; // column x is 1 in rows y and y+1
-            if (x < W && below)
-                col = load_f32<DT>(masks, base + x) == 1.f && load_f32<DT>(masks, base + W + x) == 1.f;
-            bool next = __shfl_down_sync(0xffffffffu, col, 1);
+            const bool row = y0 + i < H;
+            own[i] = row && x < W ? load_f32<DT>(masks, (view + y0 + i) * W + x) : 0.f;
+            right[i] = row && lane == 31 && x + 1 < W ? load_f32<DT>(masks, (view + y0 + i) * W + x + 1) : 0.f;
+        }
+        uint32_t prev = 0;
+#pragma unroll
+        for (int i = 0; i <= kOnesBand; ++i)
+        {
+            const bool one = own[i] == 1.f;
+            bool next = __shfl_down_sync(0xffffffffu, one, 1);
             if (lane == 31)
-                next = x + 1 < W && below && load_f32<DT>(masks, base + x + 1) == 1.f &&
-                       load_f32<DT>(masks, base + W + x + 1) == 1.f;
-            const uint32_t word = __ballot_sync(0xffffffffu, col && next);
-            if (lane == 0)
-                p.ones[row * p.WW + (x0 >> 5)] = word;
+                next = right[i] == 1.f;
+            const uint32_t pair = __ballot_sync(0xffffffffu, one && next);
+            if (i > 0 && lane == 0 && y0 + i - 1 < H)
+                p.ones[(view + y0 + i - 1) * WW + chunk] = prev & pair;
+            prev = pair;
         }
     }
 }
@@ -335,6 +353,9 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p, int64_t b0, int6
 // Ranks of the 8 corners of the cell with base corner t; false if incomplete.
 // Ranks at or beyond n (possible only when the corner pool overflowed and the
 // request is about to be rerun) count as missing, so no access leaves the pools.
+// The points (x, row) and (x + 1, row) are neighbours in the bitmap's order,
+// so when both are set their ranks are consecutive: one rank lookup per row
+// of the cell (three, the base row's rank being t) instead of seven.
 __device__ __forceinline__ bool cell_ranks(const HullPlan& p,
                                            int64_t t,
                                            int64_t n,
@@ -346,11 +367,28 @@ __device__ __forceinline__ bool cell_ranks(const HullPlan& p,
     const int64_t R = p.R;
     if (!(gx < R - 1 && gy < R - 1 && gz < R - 1))
         return false;
-    rk[0] = static_cast<uint32_t>(t);
+    const int b = static_cast<int>(gx & 63);
 #pragma unroll
-    for (int i = 1; i < 8; ++i)
-        if (!corner_rank(p, gx + (i & 1), gy + (i >> 1 & 1), gz + (i >> 2 & 1), rk[i]) || rk[i] >= n)
+    for (int q = 0; q < 4; ++q)
+    {
+        // row of corners (dy, dz) = (q & 1, q >> 1); x + 1 < R stays in the row
+        const int64_t w = ((gy + (q & 1)) + (gz + (q >> 1)) * R) * p.WR + (gx >> 6);
+        const uint64_t word = p.bitmap[w];
+        const bool next = b < 63 ? ((word >> (b + 1)) & 1ull) != 0 : (p.bitmap[w + 1] & 1ull) != 0;
+        if (!next)
             return false;
+        uint32_t r = static_cast<uint32_t>(t);
+        if (q > 0)
+        {
+            if (!((word >> b) & 1ull))
+                return false;
+            r = p.word_rank[w] + static_cast<uint32_t>(__popcll(word & ((1ull << b) - 1ull)));
+        }
+        if (r + 1 >= n)
+            return false;
+        rk[2 * q] = r;
+        rk[2 * q + 1] = r + 1;
+    }
     return true;
 }
 
@@ -511,49 +549,91 @@ __global__ void __launch_bounds__(256) export_verts_kernel(HullPlan p, float* __
 // Faces in soup order; with unique vertices they index the edge-numbered
 // vertex list, without they index the soup, which this kernel also writes.
 // Columns 1 and 2 are swapped as flip_faces does (visual_hull_cuda.cu:941-956).
-__global__ void __launch_bounds__(256) export_faces_kernel(HullPlan p, float* __restrict__ verts, int64_t* __restrict__ faces)
+// A warp takes 32 consecutive corners, whose face entries form one contiguous
+// range of the soup (soup_off is their exclusive prefix sum).  The range's
+// entries are dealt out one per lane (entry k of the range belongs to the
+// cell whose offset is the last one <= k; the cells' corner ranks are parked
+// in shared memory), parked in shared memory at their flipped position, and
+// stored with coalesced writes.  One thread per cell left three quarters of
+// the lanes idle (a quarter of the corners start an active cell, with 1 to 15
+// entries) and scattered each store over ~50 sectors.
+constexpr int kExportWarps = 8;
+
+__global__ void __launch_bounds__(32 * kExportWarps) export_faces_kernel(HullPlan p, float* __restrict__ verts, int64_t* __restrict__ faces)
 {
     __shared__ TableCache tab;
+    __shared__ int64_t stage_all[kExportWarps][32 * 15];
+    __shared__ uint32_t ranks_all[kExportWarps][32][9];
     load_tables(tab);
+    int64_t* stage = stage_all[threadIdx.x >> 5];
+    uint32_t(*ranks)[9] = ranks_all[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
     const int64_t n = p.ctr->corners;
     const float scale = __fdiv_rn(p.length, static_cast<float>(int64_t{ 1 } << p.level));
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t wb = warp * 32; wb < n; wb += nwarps * 32)
     {
-        const uint32_t code = p.codes[t];
+        const int64_t t = wb + lane;
+        const bool valid = t < n;
+        const uint32_t code = valid ? p.codes[t] : 0u;
         const int cnt = tab.count[code];
-        if (cnt == 0)
+        const unsigned act = __ballot_sync(0xffffffffu, cnt > 0);
+        if (!act)
             continue;
-        const int64_t idx = p.corners[t];
-        int64_t gx, gy, gz;
-        unpack_corner(idx, gx, gy, gz);
-        uint32_t rk[8];
-        cell_ranks(p, t, n, gx, gy, gz, rk);
-        const int64_t base = p.soup_off[t];
-        for (int j = 0; j < cnt; ++j)
+        // the warp's range of the soup starts at lane 0's offset (a multiple of 3)
+        const int64_t lo = __shfl_sync(0xffffffffu, valid ? static_cast<int64_t>(p.soup_off[t]) : int64_t{ 0 }, 0);
+        const int64_t id = cnt > 0 ? p.corners[t] : 0;
+        if (cnt > 0)
         {
-            const uint32_t e = tab.edges[code][j];
-            const int lo = static_cast<int>(e & 7u), axis = static_cast<int>(e >> 3);
-            const int64_t f = base + j;
-            const int slot = static_cast<int>(f % 3);
-            const int64_t dst = f - slot + (slot == 0 ? 0 : 3 - slot);
-            if (p.unique)
+            int64_t gx, gy, gz;
+            unpack_corner(id, gx, gy, gz);
+            uint32_t rk[8];
+            cell_ranks(p, t, n, gx, gy, gz, rk);
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                ranks[lane][i] = rk[i];
+        }
+        const int incl = warp_inclusive_scan(cnt);
+        const int excl = incl - cnt;
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        for (int k0 = 0; k0 < total; k0 += 32)
+        {
+            const int k = k0 + lane;
+            const int s = item_slot(excl, k);
+            const int es = __shfl_sync(0xffffffffu, excl, s);
+            const uint32_t cs = __shfl_sync(0xffffffffu, code, s);
+            const int64_t ids = __shfl_sync(0xffffffffu, id, s);
+            if (k < total)
             {
-                const uint32_t r1 = rk[lo];
-                faces[dst] = static_cast<int64_t>(p.vbase[r1]) + __popc(p.emask[r1] & ((1u << axis) - 1u));
-            }
-            else
-            {
-                float v[3];
-                const int hi = lo | (1 << axis);
-                edge_vertex(p, gx + (lo & 1), gy + (lo >> 1 & 1), gz + (lo >> 2 & 1), axis, p.values[rk[lo]],
-                            p.values[rk[hi]], scale, v);
-                verts[3 * f + 0] = v[0];
-                verts[3 * f + 1] = v[1];
-                verts[3 * f + 2] = v[2];
-                faces[dst] = f;
+                const uint32_t e = tab.edges[cs][k - es];
+                const int lo_corner = static_cast<int>(e & 7u), axis = static_cast<int>(e >> 3);
+                const int64_t f = lo + k;
+                const int slot = static_cast<int>(f % 3);
+                const int dst = k - slot + (slot == 0 ? 0 : 3 - slot);
+                const uint32_t r1 = ranks[s][lo_corner];
+                if (p.unique)
+                    stage[dst] = static_cast<int64_t>(p.vbase[r1]) + __popc(p.emask[r1] & ((1u << axis) - 1u));
+                else
+                {
+                    int64_t gx, gy, gz;
+                    unpack_corner(ids, gx, gy, gz);
+                    float v[3];
+                    const int hi_corner = lo_corner | (1 << axis);
+                    edge_vertex(p, gx + (lo_corner & 1), gy + (lo_corner >> 1 & 1), gz + (lo_corner >> 2 & 1), axis,
+                                p.values[r1], p.values[ranks[s][hi_corner]], scale, v);
+                    verts[3 * f + 0] = v[0];
+                    verts[3 * f + 1] = v[1];
+                    verts[3 * f + 2] = v[2];
+                    stage[dst] = f;
+                }
             }
         }
+        __syncwarp();
+        for (int i = lane; i < total; i += 32)
+            faces[lo + i] = stage[i];
+        __syncwarp();
     }
 }
 
@@ -584,8 +664,8 @@ void launch_rank_corners(const HullPlan& p, cudaStream_t s)
     const int64_t row_words = (p.R * p.R + 31) / 32;
     run_scan(RowCount{ p.rowbits }, RowEmit{ p.rowbits, p.rows }, RowEpilogue{ p.ctr }, Count{ nullptr, row_words },
              row_words, p.tile_sums, &p.ctr->scan, s);
-    run_scan(CornerCount{ p }, CornerEmit{ p }, CornerEpilogue{ p.ctr, p.corner_cap }, Count{ &p.ctr->rows, 0 },
-             p.R * p.R, p.tile_sums, &p.ctr->scan, s);
+    run_scan(CornerCount{ p }, CornerEmit{ p }, CornerEpilogue{ p.ctr, p.corner_cap }, Count{ &p.ctr->rows, 0, p.WR },
+             p.R * p.R * p.WR, p.tile_sums, &p.ctr->scan, s);
 }
 
 void launch_field(const HullPlan& p, cudaStream_t s)
@@ -593,7 +673,8 @@ void launch_field(const HullPlan& p, cudaStream_t s)
     if (p.field_ones)
     {
         bool ok = dispatch_image_dtype(p.masks_dtype, [&]<int DT>() {
-            ones_kernel<DT><<<grid_for(p.B * p.H * 32, 256), 256, 0, s>>>(p);
+            const int64_t units = p.B * ((p.H + kOnesBand - 1) / kOnesBand) * p.WW;
+            ones_kernel<DT><<<grid_for(units * 32, 256), 256, 0, s>>>(p);
         });
         if (!ok)
             throw CudaError{ cudaErrorInvalidValue, "hull field: unsupported mask dtype" };
@@ -632,7 +713,7 @@ void launch_export(const HullPlan& p, float* verts, int64_t* faces, cudaStream_t
         export_verts_kernel<<<grid, 256, 0, s>>>(p, verts);
         TH_LAUNCH_CHECK();
     }
-    export_faces_kernel<<<grid, 256, 0, s>>>(p, verts, faces);
+    export_faces_kernel<<<grid_for(p.corner_cap, 32 * kExportWarps), 32 * kExportWarps, 0, s>>>(p, verts, faces);
     TH_LAUNCH_CHECK();
 }
 

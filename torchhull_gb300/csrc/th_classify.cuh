@@ -171,20 +171,6 @@ __device__ __forceinline__ uint32_t run_or(uint32_t v, int s, int lane)
     return v;
 }
 
-// Slot owning item k: the last lane whose exclusive item offset is <= k.
-__device__ __forceinline__ int item_slot(int excl, int k)
-{
-    int s = 0;
-#pragma unroll
-    for (int step = 16; step > 0; step >>= 1)
-    {
-        const int e = __shfl_sync(0xffffffffu, excl, s + step);
-        if (s + step < 32 && e <= k)
-            s += step;
-    }
-    return s;
-}
-
 // World coordinates of the lattice of the cell idx (ravelled at resolution
 // 2^li): c + v/r * L with the product fused (visual_hull_cuda.cu:206-213);
 // v/r == v * (1/r) exactly (r = 2^k).

@@ -250,6 +250,22 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
+// Work items dealt out to a warp's lanes: lane s owns the items [excl_s,
+// excl_s + count_s) (excl a non-decreasing exclusive prefix sum over the
+// lanes).  Slot owning item k: the last lane whose exclusive offset is <= k.
+__device__ __forceinline__ int item_slot(int excl, int k)
+{
+    int s = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1)
+    {
+        const int e = __shfl_sync(0xffffffffu, excl, s + step);
+        if (s + step < 32 && e <= k)
+            s += step;
+    }
+    return s;
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_inclusive_scan(T v)
 {
@@ -303,9 +319,10 @@ struct Count
 {
     const int64_t* ptr;
     int64_t val;
+    int64_t mul = 1; // items per counted unit (with ptr)
     __device__ __forceinline__ int64_t get() const
     {
-        return ptr ? *ptr : val;
+        return ptr ? *ptr * mul : val;
     }
 };
 
