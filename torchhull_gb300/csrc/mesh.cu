@@ -204,9 +204,30 @@ __device__ __forceinline__ float view_factor(const HullPlan& p, const void* mask
     float px, py;
     to_pixel_rows(rows[0], rows[1], rows[2], wx, wy, wz, p.opengl, Hf, Wf, px, py);
     const float pad = PARTIAL ? 1.f : 0.f;
-    // 1 <= round(q) < size - 1 (half away from zero) exactly when 0.5 <= q < size - 1.5
-    if (PARTIAL && !(px >= 0.5f && px < __fsub_rn(Wf, 1.5f) && py >= 0.5f && py < __fsub_rn(Hf, 1.5f)))
-        return 1.f;
+    if constexpr (PARTIAL)
+    {
+        // 1 <= round(q) < size - 1 (half away from zero) exactly when 0.5 <= q < size - 1.5
+        if (!(px >= 0.5f && px < __fsub_rn(Wf, 1.5f) && py >= 0.5f && py < __fsub_rn(Hf, 1.5f)))
+            return 1.f;
+        // In frame q - 0.5 is exact and >= 0, so round(q - 0.5) = floor(q), in
+        // [0, size - 2]; q + 2^23 rounded down is 2^23 + floor(q) (the floats
+        // in [2^23, 2^24) are the integers).
+        const float sy = __fadd_rd(py, kTwo23), sx = __fadd_rd(px, kTwo23);
+        const int64_t y0 = __float_as_int(sy) - kTwo23Bits, x0 = __float_as_int(sx) - kTwo23Bits;
+        // all-ones footprint: exactly 1 (the weights below are in [0, 1])
+        if (p.field_ones)
+        {
+            const uint32_t word = __ldg(p.ones + (b * p.H + y0) * p.WW + (x0 >> 5));
+            if ((word >> (x0 & 31)) & 1u)
+                return 1.f;
+        }
+        const int64_t i = (b * p.H + y0) * p.W + x0;
+        const float v00 = load_f32<DT>(masks, i);
+        const float v01 = load_f32<DT>(masks, i + 1);
+        const float v10 = load_f32<DT>(masks, i + p.W);
+        const float v11 = load_f32<DT>(masks, i + p.W + 1);
+        return bilerp(v00, v10, v01, v11, __fsub_rn(py, __fsub_rn(sy, kTwo23)), __fsub_rn(px, __fsub_rn(sx, kTwo23)));
+    }
     Snapped ry, rx;
     if (!round_small(__fadd_rn(py, -0.5f), ry))
     {
@@ -230,23 +251,10 @@ __device__ __forceinline__ float view_factor(const HullPlan& p, const void* mask
         if ((word >> (x0 & 31)) & 1u)
             return 1.f;
     }
-    float v00, v10, v01, v11;
-    if (PARTIAL)
-    {
-        // in frame: round(q - 0.5) lies in [0, size - 2], so all four samples are inside
-        const int64_t i = (b * p.H + y0) * p.W + x0;
-        v00 = load_f32<DT>(masks, i);
-        v01 = load_f32<DT>(masks, i + 1);
-        v10 = load_f32<DT>(masks, i + p.W);
-        v11 = load_f32<DT>(masks, i + p.W + 1);
-    }
-    else
-    {
-        v00 = mask_sample<DT>(p, masks, b, y0, x0, pad);
-        v10 = mask_sample<DT>(p, masks, b, y0 + 1, x0, pad);
-        v01 = mask_sample<DT>(p, masks, b, y0, x0 + 1, pad);
-        v11 = mask_sample<DT>(p, masks, b, y0 + 1, x0 + 1, pad);
-    }
+    const float v00 = mask_sample<DT>(p, masks, b, y0, x0, pad);
+    const float v10 = mask_sample<DT>(p, masks, b, y0 + 1, x0, pad);
+    const float v01 = mask_sample<DT>(p, masks, b, y0, x0 + 1, pad);
+    const float v11 = mask_sample<DT>(p, masks, b, y0 + 1, x0 + 1, pad);
     const float ty = __fsub_rn(py, ry.f);
     const float tx = __fsub_rn(px, rx.f);
     return bilerp(v00, v10, v01, v11, ty, tx);
@@ -258,9 +266,9 @@ __device__ __forceinline__ float view_factor(const HullPlan& p, const void* mask
 // chunk), then per row a lane tests its column, takes its right neighbour's
 // result by a shuffle, and a ballot gives the row's "this column and the next
 // are 1" bits; a footprint word is the AND of two consecutive rows' bits.
-// Each mask row is read once, plus one row per band.  Columns x = W-1 and the
+// Each mask row is read once, plus one row per band of 8.  Columns x = W-1 and the
 // last row have no 2x2 footprint and get 0.
-constexpr int kOnesBand = 16;
+constexpr int kOnesBand = 8;
 
 template <int DT>
 __global__ void __launch_bounds__(256) ones_kernel(HullPlan p)
