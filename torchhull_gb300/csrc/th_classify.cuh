@@ -79,14 +79,27 @@ __device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sa
     const Snapped y0 = round_clamp(vminy, __fsub_rn(Hf, 1.f));
     const Snapped x1 = round_clamp(vmaxx, __fsub_rn(Wf, 1.f));
     const Snapped y1 = round_clamp(vmaxy, __fsub_rn(Hf, 1.f));
-    const float sum = box_sum(sat_b, W, x0.i, y0.i, x1.i, y1.i);
-    // float(area) of the int64 area: a product of two exact integers, rounded once
-    const float area_f = __fmul_rn(__fadd_rn(__fsub_rn(y1.f, y0.f), 1.f), __fadd_rn(__fsub_rn(x1.f, x0.f), 1.f));
     // every rounded corner inside the image (the clamps were no-ops): round(v)
     // is in [0, size - 1] exactly when v is in (-0.5, size - 0.5)
     const float hx = __fsub_rn(Wf, 0.5f), hy = __fsub_rn(Hf, 0.5f);
     const bool framed = vminx > -0.5f && vminx < hx && vmaxx > -0.5f && vmaxx < hx && vminy > -0.5f &&
                         vminy < hy && vmaxy > -0.5f && vmaxy < hy;
+    if (PARTIAL && !framed && fabsf(vminx) < 4194304.f && fabsf(vmaxx) < 4194304.f && fabsf(vminy) < 4194304.f &&
+        fabsf(vmaxy) < 4194304.f)
+    {
+        // Not "whole": with |v| < 2^22 the rounded box spans at least 2
+        // pixels per axis (v_max - v_min >= 1 and round(v + 1) >= round(v) + 1),
+        // so on an axis that leaves the image the clamp shortens it and the
+        // clamped area is below the unclamped one.  Neither empty nor object
+        // then, and the sum is not needed.
+        ViewResult res{ kNone, false };
+        if (y1.i - y0.i > 1 && x1.i - x0.i > 1)
+            res.cls = kRefine;
+        return res;
+    }
+    const float sum = box_sum(sat_b, W, x0.i, y0.i, x1.i, y1.i);
+    // float(area) of the int64 area: a product of two exact integers, rounded once
+    const float area_f = __fmul_rn(__fadd_rn(__fsub_rn(y1.f, y0.f), 1.f), __fadd_rn(__fsub_rn(x1.f, x0.f), 1.f));
     bool whole = true;
     if (PARTIAL && !framed)
     {
