@@ -43,6 +43,7 @@ __global__ void batch_init_kernel(BatchPlan bp)
     {
         bp.nodes[i] = static_cast<int64_t>(i) << kTagShift;
         bp.node_skip[i] = 0;
+        bp.node_out[i] = 0;
     }
     if (threadIdx.x == 0)
         bp.ctr->count[0] = bp.nreq;
@@ -57,16 +58,18 @@ __device__ __forceinline__ ItemResult batch_item(const BatchReq& q,
                                                  const float wy[3],
                                                  const float wz[3],
                                                  bool want_skip,
-                                                 bool skip_inside)
+                                                 bool skip_inside,
+                                                 bool want_out)
 {
     const ViewSource src = make_view_source(q.tf, q.sat, q.H, q.W);
     if constexpr (VARIANT >= 0)
-        return classify_item<(VARIANT >> 1) != 0, (VARIANT & 1) != 0>(src, b, wx, wy, wz, want_skip, skip_inside);
+        return classify_item<(VARIANT >> 1) != 0, (VARIANT & 1) != 0>(src, b, wx, wy, wz, want_skip, skip_inside,
+                                                                      want_out);
     if (q.partial)
-        return q.opengl ? classify_item<true, true>(src, b, wx, wy, wz, want_skip, skip_inside)
-                        : classify_item<true, false>(src, b, wx, wy, wz, want_skip, skip_inside);
-    return q.opengl ? classify_item<false, true>(src, b, wx, wy, wz, want_skip, skip_inside)
-                    : classify_item<false, false>(src, b, wx, wy, wz, want_skip, skip_inside);
+        return q.opengl ? classify_item<true, true>(src, b, wx, wy, wz, want_skip, skip_inside, want_out)
+                        : classify_item<true, false>(src, b, wx, wy, wz, want_skip, skip_inside, want_out);
+    return q.opengl ? classify_item<false, true>(src, b, wx, wy, wz, want_skip, skip_inside, want_out)
+                    : classify_item<false, false>(src, b, wx, wy, wz, want_skip, skip_inside, want_out);
 }
 
 // Entries of level li that were written (a pool overflow drops the rest).
@@ -114,14 +117,22 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchP
             const bool skips = work && q.skip_ok && (*q.nonbinary == 0);
             const uint32_t view_bits = q.B >= 32 ? 0xffffffffu : ((1u << q.B) - 1u);
             const uint32_t skipm = skips ? (bp.node_skip[start + pi] & view_bits) : 0u;
-            const int count = work ? (q.B - __popc(skipm)) : 0;
+            // views that see the cell out of the frame for good (partial requests)
+            const uint32_t outm = (work && q.partial) ? (bp.node_out[start + pi] & view_bits) : 0u;
+            const uint32_t skipall = skipm | outm;
+            const int count = work ? (q.B - __popc(skipall)) : 0;
             const bool last = (li == q.level - 1);
             ws.empty[lane] = 0;
             ws.refine[lane] = 0;
             ws.inside[lane] = (work && q.partial && last && skipm) ? 0xffu : 0u;
 #pragma unroll
             for (int c = 0; c < 8; ++c)
+            {
                 ws.cskip[lane][c] = 0;
+                ws.cout[lane][c] = 0;
+            }
+            // the children inherit the cell's out-of-frame views
+            ws.cout_all[lane] = outm;
             const int incl = warp_inclusive_scan(count);
             const int excl = incl - count;
             const int total = __shfl_sync(0xffffffffu, incl, 31);
@@ -131,10 +142,10 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchP
                 const int k = k0 + lane;
                 const int s = item_slot(excl, k);
                 const int es = __shfl_sync(0xffffffffu, excl, s);
-                const uint32_t ms = __shfl_sync(0xffffffffu, skipm, s);
+                const uint32_t ms = __shfl_sync(0xffffffffu, skipall, s);
                 const int64_t is = __shfl_sync(0xffffffffu, node, s);
                 const bool act = k < total;
-                ItemResult res{ 0, 0, 0, 0 };
+                ItemResult res{ 0, 0, 0, 0, 0 };
                 int b = 0;
                 bool produce = false;
                 if (act)
@@ -149,7 +160,13 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchP
                     lattice_world(qq.corner, qq.length, is & kCellMask, li, inv_rc, wx, wy, wz);
                     produce = qq.skip_ok && (*qq.nonbinary == 0) && (li + 1 < qq.level);
                     const bool skip_inside = qq.partial && (li + 1 == qq.level - 1);
-                    res = batch_item<VARIANT>(qq, b, wx, wy, wz, produce && b < 32, skip_inside);
+                    const bool want_out = qq.partial && (li + 1 < qq.level) && b < 32;
+                    res = batch_item<VARIANT>(qq, b, wx, wy, wz, produce && b < 32, skip_inside, want_out);
+                    if (res.out == 0xffu)
+                        atomicOr(&ws.cout_all[s], 1u << b);
+                    else
+                        for (uint32_t o = res.out; o; o &= o - 1)
+                            atomicOr(&ws.cout[s][__ffs(o) - 1], 1u << b);
                 }
                 const int seg = act ? s : -1 - lane;
                 const int prev_seg = __shfl_up_sync(0xffffffffu, seg, 1);
@@ -193,9 +210,13 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchP
                 if (pi < bp.skip_cap)
                 {
                     const bool produce_me = skips && (li + 1 < q.level);
+                    const bool produce_out = work && q.partial && (li + 1 < q.level);
 #pragma unroll
                     for (int c = 0; c < 8; ++c)
+                    {
                         bp.child_skip[pi * 8 + c] = produce_me ? ws.cskip[lane][c] : 0u;
+                        bp.child_out[pi * 8 + c] = produce_out ? (ws.cout[lane][c] | ws.cout_all[lane]) : 0u;
+                    }
                 }
             }
             __syncwarp();
@@ -253,6 +274,7 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchP
                     {
                         bp.nodes[out] = tag | (gx + (c & 1)) | ((gy + (c >> 1 & 1)) << sh) | ((gz + (c >> 2 & 1)) << (2 * sh));
                         bp.node_skip[out] = i < bp.skip_cap ? bp.child_skip[i * 8 + c] : 0u;
+                        bp.node_out[out] = i < bp.skip_cap ? bp.child_out[i * 8 + c] : 0u;
                     }
                     else
                         atomicOr(&ctr->overflow, 1ull);

@@ -124,8 +124,8 @@ bool is_image_dtype(int d)
 // Pools and the state of the last request of one context.
 struct HullSlot
 {
-    DevBuf tf, sat, ones, nodes, node_skip, child_masks, child_skip, tile_sums, bitmap, word_rank, rowbits, rows,
-            corners, values, codes, emask, soup_off, vbase, counters, flags;
+    DevBuf tf, sat, ones, nodes, node_skip, node_out, child_masks, child_skip, child_out, tile_sums, bitmap, word_rank,
+            rowbits, rows, corners, values, codes, emask, soup_off, vbase, counters, flags;
     int64_t node_cap = 0, corner_cap = 0, parent_cap = 0;
     HullPlan plan{};
     DevCounters* host = nullptr; // pinned copy of the counters
@@ -156,7 +156,7 @@ struct HullSlot
 
     std::vector<const DevBuf*> buffers() const
     {
-        return { &tf,     &sat,  &ones,     &nodes,     &node_skip,   &child_masks, &child_skip, &tile_sums,
+        return { &tf,     &sat,  &ones,     &nodes,     &node_skip,   &node_out,  &child_masks, &child_skip, &child_out, &tile_sums,
                  &bitmap, &word_rank, &rowbits, &rows, &corners,    &values,     &codes,
                  &emask,  &soup_off, &vbase,   &counters, &flags, &rq };
     }
@@ -268,7 +268,7 @@ namespace
 // carve, the request table, and the streams the per-request stages run on.
 struct BatchState
 {
-    DevBuf reqs, nodes, node_skip, ctr, child_masks, child_skip, block_sums;
+    DevBuf reqs, nodes, node_skip, node_out, ctr, child_masks, child_skip, child_out, block_sums;
     BatchReq* host_reqs = nullptr; // pinned
     int32_t host_reqs_cap = 0;
     BatchCounters* host_ctr = nullptr; // pinned
@@ -279,7 +279,7 @@ struct BatchState
 
     void release()
     {
-        for (DevBuf* b : { &reqs, &nodes, &node_skip, &ctr, &child_masks, &child_skip, &block_sums })
+        for (DevBuf* b : { &reqs, &nodes, &node_skip, &node_out, &ctr, &child_masks, &child_skip, &child_out, &block_sums })
             b->release();
         if (host_reqs)
             cudaFreeHost(host_reqs);
@@ -458,8 +458,10 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_one
         s.ones.ensure(sizeof(uint32_t) * std::max<int64_t>(B * H * WW, 1));
     s.nodes.ensure(sizeof(int64_t) * node_cap);
     s.node_skip.ensure(sizeof(uint32_t) * node_cap);
+    s.node_out.ensure(sizeof(uint32_t) * node_cap);
     s.child_masks.ensure(node_cap);
     s.child_skip.ensure(sizeof(uint32_t) * 8 * parent_cap);
+    s.child_out.ensure(sizeof(uint32_t) * 8 * parent_cap);
     s.flags.ensure(sizeof(unsigned int) * 4);
     const int64_t scan_items = std::max({ node_cap, corner_cap, R * R * WR });
     s.tile_sums.ensure(sizeof(unsigned long long) * ((scan_items + kScanTile - 1) / kScanTile + 1));
@@ -507,6 +509,8 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_one
     p.tile_sums = s.tile_sums.as<unsigned long long>();
     p.node_skip = s.node_skip.as<uint32_t>();
     p.child_skip = s.child_skip.as<uint32_t>();
+    p.node_out = s.node_out.as<uint32_t>();
+    p.child_out = s.child_out.as<uint32_t>();
     p.parent_cap = parent_cap;
     p.nonbinary = s.flags.as<unsigned int>();
     // exact integer box sums need every SAT sum of two entries below 2^24
@@ -831,10 +835,12 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
         bs.reqs.ensure(sizeof(BatchReq) * n);
         bs.nodes.ensure(sizeof(int64_t) * bs.node_cap);
         bs.node_skip.ensure(sizeof(uint32_t) * bs.node_cap);
+        bs.node_out.ensure(sizeof(uint32_t) * bs.node_cap);
         // view-skip masks for up to a quarter of the pool's cells in one level
         const int64_t skip_cap = std::max<int64_t>(bs.node_cap / 4, 1);
         bs.child_masks.ensure(static_cast<size_t>(bs.node_cap));
         bs.child_skip.ensure(sizeof(uint32_t) * 8 * skip_cap);
+        bs.child_out.ensure(sizeof(uint32_t) * 8 * skip_cap);
         bs.block_sums.ensure(sizeof(unsigned long long) * 8 * sm_count());
         bs.ctr.ensure(sizeof(BatchCounters));
         for (int32_t r = 0; r < n; ++r)
@@ -881,10 +887,12 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
         bp.max_level = max_level;
         bp.nodes = bs.nodes.as<int64_t>();
         bp.node_skip = bs.node_skip.as<uint32_t>();
+        bp.node_out = bs.node_out.as<uint32_t>();
         bp.node_cap = bs.node_cap;
         bp.ctr = bs.ctr.as<BatchCounters>();
         bp.child_masks = bs.child_masks.as<uint8_t>();
         bp.child_skip = bs.child_skip.as<uint32_t>();
+        bp.child_out = bs.child_out.as<uint32_t>();
         bp.skip_cap = skip_cap;
         bp.block_sums = bs.block_sums.as<unsigned long long>();
         bp.variant = -1;

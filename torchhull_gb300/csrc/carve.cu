@@ -82,6 +82,7 @@ __global__ void hull_init_kernel(HullPlan p)
         c->level_off[1] = 1;
         p.nodes[0] = 0;
         p.node_skip[0] = 0;
+        p.node_out[0] = 0;
     }
 }
 
@@ -91,11 +92,13 @@ struct LevelInfo
     int64_t n;
     const int64_t* parents;
     const uint32_t* parent_skip;
+    const uint32_t* parent_out;
     float inv_rc;
     bool last;
     bool skips;       // binary masks: skip masks are valid and may be produced
     bool produce;     // compute the children's skip masks (the next level consumes them)
     bool skip_inside; // the children's skip masks are for the last level (partial)
+    bool produce_out; // compute the children's out-of-frame masks (partial; the next level consumes them)
 };
 
 __device__ __forceinline__ LevelInfo level_info(const HullPlan& p, int li, bool partial)
@@ -106,12 +109,14 @@ __device__ __forceinline__ LevelInfo level_info(const HullPlan& p, int li, bool 
     const int64_t off = ctr->level_off[li];
     L.parents = p.nodes + off;
     L.parent_skip = p.node_skip + off;
+    L.parent_out = p.node_out + off;
     L.inv_rc = __int_as_float((127 - (li + 1)) << 23); // 2^-(li + 1), exact
     L.last = (li == p.level - 1);
     L.skips = p.skip_ok && (*p.nonbinary == 0);
     // the children are parents of the next level, which uses the item kernel
     L.produce = L.skips && (li + 1 < p.level) && p.carve_variant[li + 1] == 1;
     L.skip_inside = partial && (li + 1 == p.level - 1);
+    L.produce_out = partial && (li + 1 < p.level) && p.carve_variant[li + 1] == 1;
     return L;
 }
 
@@ -135,11 +140,12 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_views_kernel
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     // skip masks can come out of a ballot only when lane == view (<= 32 views)
     const bool produce = L.produce && LANES == 32 && p.B <= 32;
+    const bool produce_out = L.produce_out && LANES == 32 && p.B <= 32;
     for (int64_t base = warp * G; base < L.n; base += nwarps * G)
     {
         const int64_t pi = base + grp;
         const bool valid = pi < L.n;
-        uint32_t empty = 0, refine = 0, inside = 0, skip = 0;
+        uint32_t empty = 0, refine = 0, inside = 0, skip = 0, outb = 0;
         if (valid)
         {
             float wx[3], wy[3], wz[3];
@@ -147,19 +153,27 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_views_kernel
             const ViewSource src = make_view_source(p.tf, p.sat, p.H, p.W);
             for (int64_t b = sub; b < p.B; b += LANES)
             {
-                const ItemResult r = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, produce, L.skip_inside);
+                const ItemResult r =
+                        classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, produce, L.skip_inside, produce_out);
                 empty |= r.empty;
                 refine |= r.refine;
                 inside |= r.inside;
                 skip |= r.skip;
+                outb |= r.out;
             }
         }
-        uint32_t cskip[8];
+        uint32_t cskip[8], cout[8];
         if (produce)
         {
 #pragma unroll
             for (int c = 0; c < 8; ++c)
                 cskip[c] = __ballot_sync(0xffffffffu, (skip >> c) & 1u);
+        }
+        if (produce_out)
+        {
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                cout[c] = __ballot_sync(0xffffffffu, (outb >> c) & 1u);
         }
 #pragma unroll
         for (int off = LANES / 2; off > 0; off >>= 1)
@@ -175,7 +189,10 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_views_kernel
             {
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
+                {
                     p.child_skip[pi * 8 + c] = produce ? cskip[c] : 0u;
+                    p.child_out[pi * 8 + c] = produce_out ? cout[c] : 0u;
+                }
             }
         }
     }
@@ -204,7 +221,10 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel
         const bool valid = lane < ppw && pi < L.n;
         const int64_t idx = valid ? L.parents[pi] : 0;
         const uint32_t skipm = (valid && L.skips) ? (L.parent_skip[pi] & view_bits) : 0u;
-        const int count = valid ? (B - __popc(skipm)) : 0;
+        // views that see the parent out of the frame for good (partial mode)
+        const uint32_t outm = (valid && PARTIAL) ? (L.parent_out[pi] & view_bits) : 0u;
+        const uint32_t skipall = skipm | outm;
+        const int count = valid ? (B - __popc(skipall)) : 0;
         ws.empty[lane] = 0;
         ws.refine[lane] = 0;
         // a skipped view before the last level (partial mode) is one where
@@ -212,7 +232,12 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel
         ws.inside[lane] = (PARTIAL && L.last && skipm) ? 0xffu : 0u;
 #pragma unroll
         for (int c = 0; c < 8; ++c)
+        {
             ws.cskip[lane][c] = 0;
+            ws.cout[lane][c] = 0;
+        }
+        // the children inherit the parent's out-of-frame views
+        ws.cout_all[lane] = outm;
         const int incl = warp_inclusive_scan(count);
         const int excl = incl - count;
         const int total = __shfl_sync(0xffffffffu, incl, 31);
@@ -230,9 +255,9 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel
                     s += step;
             }
             const int es = __shfl_sync(0xffffffffu, excl, s);
-            const uint32_t ms = __shfl_sync(0xffffffffu, skipm, s);
+            const uint32_t ms = __shfl_sync(0xffffffffu, skipall, s);
             const int64_t is = __shfl_sync(0xffffffffu, idx, s);
-            ItemResult res{ 0, 0, 0, 0 };
+            ItemResult res{ 0, 0, 0, 0, 0 };
             int b = 0;
             const bool act = k < total;
             if (act)
@@ -244,7 +269,13 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel
                 float wx[3], wy[3], wz[3];
                 lattice_world(p.rq->corner, p.rq->length, is, li, L.inv_rc, wx, wy, wz);
                 const ViewSource src = make_view_source(p.tf, p.sat, p.H, p.W);
-                res = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, L.produce && b < 32, L.skip_inside);
+                res = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, L.produce && b < 32, L.skip_inside,
+                                                     L.produce_out && b < 32);
+                if (res.out == 0xffu)
+                    atomicOr(&ws.cout_all[s], 1u << b);
+                else
+                    for (uint32_t o = res.out; o; o &= o - 1)
+                        atomicOr(&ws.cout[s][__ffs(o) - 1], 1u << b);
             }
             const int seg = act ? s : -1 - lane;
             const int prev_seg = __shfl_up_sync(0xffffffffu, seg, 1);
@@ -280,7 +311,10 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel
             {
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
+                {
                     p.child_skip[pi * 8 + c] = L.produce ? ws.cskip[lane][c] : 0u;
+                    p.child_out[pi * 8 + c] = L.produce_out ? (ws.cout[lane][c] | ws.cout_all[lane]) : 0u;
+                }
             }
         }
         __syncwarp();
@@ -321,6 +355,7 @@ struct ChildEmit
                 {
                     p.nodes[out] = (gx + (k & 1)) | ((gy + (k >> 1 & 1)) << sh) | ((gz + (k >> 2 & 1)) << (2 * sh));
                     p.node_skip[out] = has_skip ? p.child_skip[i * 8 + k] : 0u;
+                    p.node_out[out] = has_skip ? p.child_out[i * 8 + k] : 0u;
                 }
                 ++out;
             }

@@ -45,6 +45,7 @@ struct BatchPlan
     int32_t max_level;
     int64_t* nodes; // level lists back to back (level i starts after levels < i)
     uint32_t* node_skip;
+    uint32_t* node_out; // out-of-frame views (HullPlan::node_out)
     int64_t node_cap;
     BatchCounters* ctr;
     // (partial << 1) | opengl when every request shares it, -1 otherwise
@@ -53,6 +54,7 @@ struct BatchPlan
     // children's view-skip masks for the first skip_cap cells
     uint8_t* child_masks;  // [node_cap]
     uint32_t* child_skip;  // [skip_cap * 8]
+    uint32_t* child_out;   // [skip_cap * 8]
     int64_t skip_cap;
     unsigned long long* block_sums; // [grid size] children per block
 };

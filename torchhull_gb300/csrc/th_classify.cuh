@@ -152,13 +152,30 @@ __device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sa
 struct ItemResult
 {
     uint32_t empty, refine, inside, skip; // 8-bit child masks
+    uint32_t out;                         // children out of the frame for good (partial mode, want_out)
 };
+
+// Partial mode: a child box (from corners all in front of the camera) more
+// than 2 pixels outside the image on one side, with every coordinate below
+// 2^21 in magnitude.  Every descendant's corners project into this box up to
+// rounding errors far below a pixel, so every descendant's box leaves the
+// frame on that side too: never whole, a clamped extent of one pixel there
+// (not refined), no corner in frame (not inside).  Such a view contributes
+// nothing to any descendant and is skipped below.
+__device__ __forceinline__ bool box_out(const Box& bb, float Hf, float Wf)
+{
+    const float lim = 2097152.f;
+    return (bb.maxx < -2.f || bb.minx > __fadd_rn(Wf, 1.f) || bb.maxy < -2.f || bb.miny > __fadd_rn(Hf, 1.f)) &&
+           fabsf(bb.minx) < lim && fabsf(bb.maxx) < lim && fabsf(bb.miny) < lim && fabsf(bb.maxy) < lim;
+}
 
 // Shared-memory accumulators of one warp's chunk of parents (one slot each).
 struct WarpSlots
 {
     uint32_t empty[32], refine[32], inside[32];
     uint32_t cskip[32][8];
+    // out-of-frame view masks of the children: per child, and for all 8
+    uint32_t cout[32][8], cout_all[32];
 };
 
 // Position of the j-th set bit of m (j < popc(m)).
@@ -225,7 +242,8 @@ __device__ __forceinline__ ViewSource make_view_source(const float* tf, const fl
 
 // One (parent, view) item: the parent's lattice projected into view b.
 // want_skip: compute the children's skip bits; skip_inside: the skip rule also
-// needs the child's corners two pixels inside the frame.
+// needs the child's corners two pixels inside the frame; want_out (partial
+// mode): compute the children's out-of-frame bits (box_out).
 template <bool PARTIAL, bool OPENGL>
 __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                                                     int64_t b,
@@ -233,7 +251,8 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                                                     const float wy[3],
                                                     const float wz[3],
                                                     bool want_skip,
-                                                    bool skip_inside)
+                                                    bool skip_inside,
+                                                    bool want_out = false)
 {
     const int32_t H = static_cast<int32_t>(p.H), W = static_cast<int32_t>(p.W);
     const float Hf = p.Hf, Wf = p.Wf;
@@ -245,7 +264,8 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
     const float* sat_b = p.sat + b * p.H * p.W;
     const float in_hx = __fsub_rn(Wf, 1.5f), in_hy = __fsub_rn(Hf, 1.5f);
     const float in2_hx = __fsub_rn(Wf, 2.5f), in2_hy = __fsub_rn(Hf, 2.5f);
-    ItemResult out{ 0, 0, 0, 0 };
+    ItemResult out{ 0, 0, 0, 0, 0 };
+    want_out = PARTIAL && want_out;
     Box prev[4];
     uint32_t prev_in = 0, prev_in2 = 0, prev_front = 0;
     // Rolled (the default), the plane loop keeps one copy of the plane's code,
@@ -290,7 +310,7 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                     px[k] = __fsub_rn(nx, 0.5f);
                     py[k] = __fsub_rn(ny, 0.5f);
                 }
-                if (want_skip && cd > 0.f)
+                if ((want_skip || want_out) && cd > 0.f)
                     front9 |= 1u << k;
                 if (PARTIAL)
                 {
@@ -331,8 +351,11 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                 const uint32_t bit = 1u << (c + 4 * (z - 1));
                 const bool front = (prev_front & cur_front & cbit) != 0;
                 const bool in2 = (prev_in2 & cur_in2 & cbit) != 0;
-                const ViewResult r = classify_view<PARTIAL>(sat_b, H, W, Hf, Wf, merge(prev[c], cur[c]),
+                const Box cb = merge(prev[c], cur[c]);
+                const ViewResult r = classify_view<PARTIAL>(sat_b, H, W, Hf, Wf, cb,
                                                             want_skip && front && (!skip_inside || in2));
+                if (want_out && front && box_out(cb, Hf, Wf))
+                    out.out |= bit;
                 if (r.cls == kEmpty)
                     out.empty |= bit;
                 else if (r.cls == kRefine)

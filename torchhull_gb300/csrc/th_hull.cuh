@@ -68,6 +68,13 @@ struct HullPlan
     // the same masks for the 8 children of each parent of the current level.
     uint32_t* node_skip;  // [node_cap]
     uint32_t* child_skip; // [parent_cap * 8]
+    // Out-of-frame views (partial mode): node_out[k] has bit b when node k's
+    // box in view b lies more than 2 pixels outside the image (box_out); no
+    // descendant's item in view b can change anything, so the item kernel
+    // skips it and the children inherit the bit.  child_out: the same for
+    // the 8 children of each parent of the current level.
+    uint32_t* node_out;   // [node_cap]
+    uint32_t* child_out;  // [parent_cap * 8]
     int64_t parent_cap;
     // carve kernel per parent level: 0 = views over lanes, 1 = (parent, view) items
     uint8_t carve_variant[kMaxLevel];

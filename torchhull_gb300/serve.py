@@ -51,7 +51,7 @@ def estimate_bytes(req: HullRequest) -> int:
     parents = min(_max_nodes(L), 1 << 22)
     sat = 4 * B * H * W
     ones = 4 * B * H * ((W + 31) // 32)
-    node_pool = nodes * (8 + 4 + 1) + parents * 32
+    node_pool = nodes * (8 + 4 + 4 + 1) + parents * 64
     corner_pool = corners * (8 + 4 + 1 + 1 + 4 + 4)
     bitmap = R * R * WR * (8 + 4) + R * R * 4 + (R * R + 31) // 32 * 4
     return int(inputs + sat + ones + node_pool + corner_pool + bitmap)
