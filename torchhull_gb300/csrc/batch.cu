@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchP
                     float wx[3], wy[3], wz[3];
                     lattice_world(qq.corner, qq.length, is & kCellMask, li, inv_rc, wx, wy, wz);
                     produce = qq.skip_ok && (*qq.nonbinary == 0) && (li + 1 < qq.level);
-                    const bool skip_inside = qq.partial && (li + 1 == qq.level - 1);
+                    const bool skip_inside = qq.partial != 0;
                     const bool want_out = qq.partial && (li + 1 < qq.level) && b < 32;
                     res = batch_item<VARIANT>(qq, b, wx, wy, wz, produce && b < 32, skip_inside, want_out);
                     if (res.out == 0xffu)
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchP
 #pragma unroll
                     for (int c = 0; c < 8; ++c)
                     {
-                        bp.child_skip[pi * 8 + c] = produce_me ? ws.cskip[lane][c] : 0u;
+                        bp.child_skip[pi * 8 + c] = produce_me ? (ws.cskip[lane][c] | skipm) : 0u;
                         bp.child_out[pi * 8 + c] = produce_out ? (ws.cout[lane][c] | ws.cout_all[lane]) : 0u;
                     }
                 }

@@ -25,16 +25,22 @@
 //    merged in shared memory.  Best when many views are skipped.
 // The host picks one per level (autotuned by measuring both).
 //
-// View skipping (binary masks).  When a child's pixel box grown by one pixel
-// lies inside the image and holds only ones, the child's own children are
-// "object" in that view too: their corners project into the child's box up to
-// rounding errors far below a pixel, so their rounded boxes stay inside the
-// grown box, every pixel there is 1, and "object" contributes nothing to the
-// decision.  The child records the view in its skip mask and the item kernel
-// never evaluates it for its children.  Before the last level in partial mode
-// a skipped view must also report "fully inside", so there the rule also
-// requires every corner of the child to round at least two pixels inside the
-// frame.  All corners must be in front of the camera for any of this.
+// View skipping (binary masks).  When a child's pixel box grown by two pixels
+// lies inside the image and holds only ones, every descendant of the child is
+// "object" in that view: the descendants' corners project into the child's
+// box up to rounding errors far below a pixel, so their rounded boxes stay
+// within one pixel of the child's, their boxes grown by one pixel stay inside
+// the grown box, every pixel there is 1, and "object" contributes nothing to
+// the decision.  The child records the view in its skip mask, its children
+// inherit the mask, and the item kernel never evaluates the view for any of
+// them.  In partial mode a skipped view must also report "fully inside" at the
+// last level, so the rule also requires every corner of the child to round at
+// least two pixels inside the frame.  All corners must be in front of the
+// camera for any of this.
+//
+// Out-of-frame views (partial masks).  A child box more than two pixels
+// outside the image (box_out) can change nothing for any descendant; the view
+// goes into the child's out mask, is inherited and skipped the same way.
 //
 // Conversions: the reference converts the rounded pixel coordinates to int64
 // (glm::i64vec2).  On GB300 64-bit float<->int conversions run on the FP64
@@ -97,7 +103,7 @@ struct LevelInfo
     bool last;
     bool skips;       // binary masks: skip masks are valid and may be produced
     bool produce;     // compute the children's skip masks (the next level consumes them)
-    bool skip_inside; // the children's skip masks are for the last level (partial)
+    bool skip_inside; // partial mode: the skip rule also wants the corners in frame
     bool produce_out; // compute the children's out-of-frame masks (partial; the next level consumes them)
 };
 
@@ -115,7 +121,7 @@ __device__ __forceinline__ LevelInfo level_info(const HullPlan& p, int li, bool 
     L.skips = p.skip_ok && (*p.nonbinary == 0);
     // the children are parents of the next level, which uses the item kernel
     L.produce = L.skips && (li + 1 < p.level) && p.carve_variant[li + 1] == 1;
-    L.skip_inside = partial && (li + 1 == p.level - 1);
+    L.skip_inside = partial;
     L.produce_out = partial && (li + 1 < p.level) && p.carve_variant[li + 1] == 1;
     return L;
 }
@@ -187,10 +193,12 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_views_kernel
             store_parent(p, L, pi, empty, refine, inside, PARTIAL);
             if (pi < p.parent_cap)
             {
+                // the children inherit the parent's skip views (all descendants are object there)
+                const uint32_t inherited = produce && L.skips ? L.parent_skip[pi] : 0u;
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
                 {
-                    p.child_skip[pi * 8 + c] = produce ? cskip[c] : 0u;
+                    p.child_skip[pi * 8 + c] = produce ? (cskip[c] | inherited) : 0u;
                     p.child_out[pi * 8 + c] = produce_out ? cout[c] : 0u;
                 }
             }
@@ -312,7 +320,7 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
                 {
-                    p.child_skip[pi * 8 + c] = L.produce ? ws.cskip[lane][c] : 0u;
+                    p.child_skip[pi * 8 + c] = L.produce ? (ws.cskip[lane][c] | skipm) : 0u;
                     p.child_out[pi * 8 + c] = L.produce_out ? (ws.cout[lane][c] | ws.cout_all[lane]) : 0u;
                 }
             }

@@ -134,13 +134,13 @@ __device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sa
         res.cls = kObject;
     else if (!PARTIAL || (y1.i - y0.i > 1 && x1.i - x0.i > 1))
         res.cls = kRefine;
-    if (want_skip && res.cls == kObject && framed && x0.i >= 1 && y0.i >= 1 && x1.i <= W - 2 && y1.i <= H - 2 &&
+    if (want_skip && res.cls == kObject && framed && x0.i >= 2 && y0.i >= 2 && x1.i <= W - 3 && y1.i <= H - 3 &&
         x0.i <= x1.i && y0.i <= y1.i)
     {
-        // the box grown by one pixel is inside the image: all ones there?
-        const int32_t gx0 = x0.i - 1, gy0 = y0.i - 1, gx1 = x1.i + 1, gy1 = y1.i + 1;
+        // the box grown by two pixels is inside the image: all ones there?
+        const int32_t gx0 = x0.i - 2, gy0 = y0.i - 2, gx1 = x1.i + 2, gy1 = y1.i + 2;
         const float grown = box_sum(sat_b, W, gx0, gy0, gx1, gy1);
-        res.skip = grown == __fmul_rn(__fadd_rn(__fsub_rn(y1.f, y0.f), 3.f), __fadd_rn(__fsub_rn(x1.f, x0.f), 3.f));
+        res.skip = grown == __fmul_rn(__fadd_rn(__fsub_rn(y1.f, y0.f), 5.f), __fadd_rn(__fsub_rn(x1.f, x0.f), 5.f));
     }
     return res;
 }

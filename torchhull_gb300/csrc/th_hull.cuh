@@ -61,10 +61,10 @@ struct HullPlan
     uint8_t* child_masks; // one byte per parent of the current level
     unsigned long long* tile_sums;
     // View skipping (binary masks only).  node_skip[k] has bit b (b < 32) set
-    // when view b need not be evaluated for the children of node k: the
-    // node's pixel box grown by one pixel lies inside the image and holds only
-    // ones, so every child is "object" there (and, for a parent of the last
-    // level in partial mode, also fully inside the frame).  child_skip holds
+    // when view b need not be evaluated for any descendant of node k: the
+    // box of node k or of one of its ancestors, grown by two pixels, lies
+    // inside the image and holds only ones, so every descendant is "object"
+    // there (and, in partial mode, fully inside the frame).  child_skip holds
     // the same masks for the 8 children of each parent of the current level.
     uint32_t* node_skip;  // [node_cap]
     uint32_t* child_skip; // [parent_cap * 8]
