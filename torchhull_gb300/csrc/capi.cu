@@ -124,8 +124,8 @@ bool is_image_dtype(int d)
 // Pools and the state of the last request of one context.
 struct HullSlot
 {
-    DevBuf tf, sat, ones, nodes, node_skip, node_out, child_masks, child_skip, child_out, tile_sums, bitmap, word_rank,
-            rowbits, rows, corners, values, codes, emask, soup_off, vbase, counters, flags;
+    DevBuf tf, sat, ones, cell_masks, nodes, node_skip, node_out, child_masks, child_skip, child_out, tile_sums, bitmap,
+            word_rank, rowbits, rows, corners, values, codes, emask, soup_off, vbase, counters, flags;
     int64_t node_cap = 0, corner_cap = 0, parent_cap = 0;
     HullPlan plan{};
     DevCounters* host = nullptr; // pinned copy of the counters
@@ -156,7 +156,7 @@ struct HullSlot
 
     std::vector<const DevBuf*> buffers() const
     {
-        return { &tf,     &sat,  &ones,     &nodes,     &node_skip,   &node_out,  &child_masks, &child_skip, &child_out, &tile_sums,
+        return { &tf,     &sat,  &ones,  &cell_masks,   &nodes,     &node_skip,   &node_out,  &child_masks, &child_skip, &child_out, &tile_sums,
                  &bitmap, &word_rank, &rowbits, &rows, &corners,    &values,     &codes,
                  &emask,  &soup_off, &vbase,   &counters, &flags, &rq };
     }
@@ -516,6 +516,14 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_one
     // exact integer box sums need every SAT sum of two entries below 2^24
     p.skip_ok = B > 0 && H > 0 && W > 0 && H * W <= (int64_t{ 1 } << 23);
     p.field_ones = field_ones && B > 0 && H > 0 && W > 0;
+    // the cell-mask table of level L-1, up to 2^27 cells (512 MB: level 10)
+    p.cell_masks = nullptr;
+    if (!batch_slot && field_ones && L >= 1 && 3 * (L - 1) <= 27 && (p.partial || p.skip_ok))
+    {
+        if (s.cell_masks.ensure(sizeof(uint32_t) * (int64_t{ 1 } << (3 * (L - 1)))))
+            TH_CUDA(cudaMemsetAsync(s.cell_masks.p, 0, s.cell_masks.bytes, st));
+        p.cell_masks = s.cell_masks.as<uint32_t>();
+    }
     p.ones = field_ones ? s.ones.as<uint32_t>() : nullptr;
     p.WW = WW;
     p.R = R;

@@ -358,6 +358,143 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p, int64_t b0, int6
     }
 }
 
+// The cell-mask table (HullPlan::cell_masks): every cell of level L-1
+// writes its skip and out-of-frame views (set) or 0 (clear).
+__global__ void __launch_bounds__(256) cell_masks_kernel(HullPlan p, bool set)
+{
+    const DevCounters* c = p.ctr;
+    const int li = p.level - 1;
+    const int64_t n = c->level_count[li];
+    const int64_t off = c->level_off[li];
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride)
+        p.cell_masks[p.nodes[off + k]] = set ? (p.node_skip[off + k] | p.node_out[off + k]) : 0u;
+}
+
+// Views of a corner whose field factor is exactly 1: the cell-mask entry of
+// the level L-1 cell (x >> 1, y >> 1, z >> 1), whose lattice holds the corner
+// (0 when the corner lies on the far faces of the grid).
+__device__ __forceinline__ uint32_t corner_view_mask(const HullPlan& p, int64_t gx, int64_t gy, int64_t gz)
+{
+    const int li = p.level - 1;
+    const int64_t cx = gx >> 1, cy = gy >> 1, cz = gz >> 1, r = int64_t{ 1 } << li;
+    if (cx >= r || cy >= r || cz >= r)
+        return 0u;
+    return p.cell_masks[cx | (cy << li) | (cz << (2 * li))];
+}
+
+// Position of the set bit of m with j set bits below it (j < popc(m)).
+__device__ __forceinline__ int nth_set_bit(uint32_t m, int j)
+{
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w > 0; w >>= 1)
+    {
+        const uint32_t low = m & ((1u << w) - 1u);
+        const int c = __popc(low);
+        if (j >= c)
+        {
+            j -= c;
+            pos += w;
+            m >>= w;
+        }
+        else
+            m = low;
+    }
+    return pos;
+}
+
+constexpr int kMaskedWarps = 8;
+
+// The field with the cell masks, for the views [b0, b1) (at most 32): the
+// views of a corner's mask are left out of its product (x * 1 == x); the
+// remaining (corner, view) items of a warp's 32 corners are dealt out to its
+// lanes, the factors parked in shared memory, and each lane multiplies its
+// corner's factors in ascending view order, the reference's order.  A warp
+// whose corners skip nothing walks the views directly, one corner per lane.
+template <int DT, bool PARTIAL>
+__global__ void __launch_bounds__(32 * kMaskedWarps) field_masked_kernel(HullPlan p, int64_t b0, int64_t b1)
+{
+    __shared__ float4 rows[32][3];
+    __shared__ float fac_all[kMaskedWarps][32][33];
+    const int nv = static_cast<int>(b1 - b0);
+    for (int i = threadIdx.x; i < 3 * nv; i += blockDim.x)
+    {
+        const int v = i / 3, r = i - 3 * (i / 3);
+        const int row = r < 2 ? r : (p.opengl ? 3 : 2);
+        rows[v][r] = *reinterpret_cast<const float4*>(p.tf + 16 * (b0 + v) + 4 * row);
+    }
+    __syncthreads();
+    float(*fac)[33] = fac_all[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int64_t n = p.ctr->corners;
+    const float inv_rc = __fdiv_rn(1.f, static_cast<float>(p.R - 1)); // exact: a power of two
+    const float Hf = small_i2f(static_cast<int32_t>(p.H)), Wf = small_i2f(static_cast<int32_t>(p.W));
+    const float cx = p.rq->corner[0], cy = p.rq->corner[1], cz = p.rq->corner[2], length = p.rq->length;
+    const void* masks = p.rq->masks;
+    const uint32_t vb = nv >= 32 ? 0xffffffffu : ((1u << nv) - 1u);
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < n; base += nwarps * 32)
+    {
+        const int64_t t = base + lane;
+        const bool valid = t < n;
+        float wx = 0.f, wy = 0.f, wz = 0.f, value = 1.f;
+        uint32_t skip = 0;
+        if (valid)
+        {
+            int64_t gx, gy, gz;
+            unpack_corner(p.corners[t], gx, gy, gz);
+            // c + v/r * L fused (visual_hull_cuda.cu:444-448), as in field_kernel
+            wx = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gx)), inv_rc), length, cx);
+            wy = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gy)), inv_rc), length, cy);
+            wz = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gz)), inv_rc), length, cz);
+            if (b0 == 0)
+                skip = corner_view_mask(p, gx, gy, gz) & vb;
+            else
+                value = p.values[t];
+        }
+        if (!__any_sync(0xffffffffu, skip != 0))
+        {
+            if (valid)
+            {
+#pragma unroll 4
+                for (int v = 0; v < nv; ++v)
+                    value = __fmul_rn(value, view_factor<DT, PARTIAL>(p, masks, b0 + v, rows[v], wx, wy, wz, Hf, Wf));
+                p.values[t] = value;
+            }
+            continue;
+        }
+        const uint32_t active = valid ? (vb & ~skip) : 0u;
+        const int count = __popc(active);
+        const int incl = warp_inclusive_scan(count);
+        const int excl = incl - count;
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        for (int k0 = 0; k0 < total; k0 += 32)
+        {
+            const int k = k0 + lane;
+            const int s = item_slot(excl, k);
+            const int es = __shfl_sync(0xffffffffu, excl, s);
+            const uint32_t as = __shfl_sync(0xffffffffu, active, s);
+            const float sx = __shfl_sync(0xffffffffu, wx, s);
+            const float sy = __shfl_sync(0xffffffffu, wy, s);
+            const float sz = __shfl_sync(0xffffffffu, wz, s);
+            if (k < total)
+            {
+                const int j = k - es;
+                const int v = nth_set_bit(as, j);
+                fac[s][j] = view_factor<DT, PARTIAL>(p, masks, b0 + v, rows[v], sx, sy, sz, Hf, Wf);
+            }
+        }
+        __syncwarp();
+        for (int j = 0; j < count; ++j)
+            value = __fmul_rn(value, fac[lane][j]);
+        __syncwarp();
+        if (valid)
+            p.values[t] = value;
+    }
+}
+
 // Ranks of the 8 corners of the cell with base corner t; false if incomplete.
 // Ranks at or beyond n (possible only when the corner pool overflowed and the
 // request is about to be rerun) count as missing, so no access leaves the pools.
@@ -687,6 +824,31 @@ void launch_field(const HullPlan& p, cudaStream_t s)
         if (!ok)
             throw CudaError{ cudaErrorInvalidValue, "hull field: unsupported mask dtype" };
         TH_LAUNCH_CHECK();
+    }
+    if (p.cell_masks)
+    {
+        const int64_t cells = p.level >= 1 ? (int64_t{ 1 } << (3 * (p.level - 1))) : 1;
+        const int mgrid = grid_for(cells < p.node_cap ? cells : p.node_cap, 256);
+        cell_masks_kernel<<<mgrid, 256, 0, s>>>(p, true);
+        TH_LAUNCH_CHECK();
+        const int grid = grid_for(p.corner_cap, 32 * kMaskedWarps);
+        // at least one launch, so that B == 0 still writes the empty product 1
+        for (int64_t b0 = 0; b0 == 0 || b0 < p.B; b0 += 32)
+        {
+            const int64_t b1 = b0 + 32 < p.B ? b0 + 32 : p.B;
+            bool ok = dispatch_image_dtype(p.masks_dtype, [&]<int DT>() {
+                if (p.partial)
+                    field_masked_kernel<DT, true><<<grid, 32 * kMaskedWarps, 0, s>>>(p, b0, b1);
+                else
+                    field_masked_kernel<DT, false><<<grid, 32 * kMaskedWarps, 0, s>>>(p, b0, b1);
+            });
+            if (!ok)
+                throw CudaError{ cudaErrorInvalidValue, "hull field: unsupported mask dtype" };
+            TH_LAUNCH_CHECK();
+        }
+        cell_masks_kernel<<<mgrid, 256, 0, s>>>(p, false);
+        TH_LAUNCH_CHECK();
+        return;
     }
     const int grid = grid_for(p.corner_cap, 256);
     // at least one launch, so that B == 0 still writes the empty product 1

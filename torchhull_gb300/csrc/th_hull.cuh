@@ -88,6 +88,14 @@ struct HullPlan
     bool field_ones;
     uint32_t* ones; // [B*H*WW]
     int64_t WW;
+    // Field masks: the skip and out-of-frame views of the cells of the last
+    // carve level (the parents of the leaves) hold for all their descendants,
+    // so for every mesh corner that is one of their lattice points the field
+    // factor of those views is exactly 1 (a footprint of four ones with
+    // weights in [0, 1], or a point out of the frame).  cell_masks is a dense
+    // table over the cells of level L-1, scattered before the field and
+    // cleared after it (nullptr: no table, every pair is evaluated).
+    uint32_t* cell_masks; // [8^(L-1)]
     // corner grid: R^3 points, one bit each, rows of WR 64-bit words (x fastest)
     int64_t R, WR;
     uint64_t* bitmap;     // [R*R*WR]
