@@ -313,6 +313,31 @@ __global__ void __launch_bounds__(256) batch_mark_kernel(BatchPlan bp)
     }
 }
 
+// The cells of level L-1 of every request with a cell-mask table write their
+// skip and out-of-frame views into it (set) or 0 (clear).
+__global__ void __launch_bounds__(256) batch_cell_masks_kernel(BatchPlan bp, bool set)
+{
+    int64_t starts[kMaxLevel + 2];
+    int64_t s = 0;
+    for (int li = 0; li <= bp.max_level; ++li)
+    {
+        starts[li] = s;
+        s += level_entries(bp, li, s);
+    }
+    const int64_t total = s;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride)
+    {
+        int li = 0;
+        while (li < bp.max_level && starts[li + 1] <= t)
+            ++li;
+        const int64_t node = bp.nodes[t];
+        const BatchReq& q = bp.reqs[static_cast<int>(node >> kTagShift)];
+        if (q.cell_masks && li == q.level - 1)
+            q.cell_masks[node & kCellMask] = set ? (bp.node_skip[t] | bp.node_out[t]) : 0u;
+    }
+}
+
 } // namespace
 
 void launch_batch_init(const BatchPlan& bp, cudaStream_t s)
@@ -358,6 +383,12 @@ void launch_batch_carve(const BatchPlan& bp, cudaStream_t s)
 void launch_batch_mark(const BatchPlan& bp, cudaStream_t s)
 {
     batch_mark_kernel<<<grid_for(bp.node_cap, 256), 256, 0, s>>>(bp);
+    TH_LAUNCH_CHECK();
+}
+
+void launch_batch_cell_masks(const BatchPlan& bp, bool set, cudaStream_t s)
+{
+    batch_cell_masks_kernel<<<grid_for(bp.node_cap, 256), 256, 0, s>>>(bp, set);
     TH_LAUNCH_CHECK();
 }
 

@@ -518,7 +518,8 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_one
     p.field_ones = field_ones && B > 0 && H > 0 && W > 0;
     // the cell-mask table of level L-1, up to 2^27 cells (512 MB: level 10)
     p.cell_masks = nullptr;
-    if (!batch_slot && field_ones && L >= 1 && 3 * (L - 1) <= 27 && (p.partial || p.skip_ok))
+    p.own_cell_masks = !batch_slot;
+    if (field_ones && L >= 1 && 3 * (L - 1) <= 27 && (p.partial || p.skip_ok))
     {
         if (s.cell_masks.ensure(sizeof(uint32_t) * (int64_t{ 1 } << (3 * (L - 1)))))
             TH_CUDA(cudaMemsetAsync(s.cell_masks.p, 0, s.cell_masks.bytes, st));
@@ -887,6 +888,7 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
             q.rowbits = p.rowbits;
             q.R = p.R;
             q.WR = p.WR;
+            q.cell_masks = p.cell_masks;
         }
         TH_CUDA(cudaMemcpyAsync(bs.reqs.p, bs.host_reqs, sizeof(BatchReq) * n, cudaMemcpyHostToDevice, st));
         BatchPlan bp{};
@@ -915,6 +917,7 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
         launch_batch_init(bp, st);
         launch_batch_carve(bp, st);
         launch_batch_mark(bp, st);
+        launch_batch_cell_masks(bp, true, st);
         // per-request stages, spread over the streams
         TH_CUDA(cudaEventRecord(bs.fork, st));
         for (int i = 0; i < nstreams; ++i)
@@ -932,6 +935,7 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
             TH_CUDA(cudaEventRecord(bs.joins[i], bs.streams[i]));
             TH_CUDA(cudaStreamWaitEvent(st, bs.joins[i], 0));
         }
+        launch_batch_cell_masks(bp, false, st);
         TH_CUDA(cudaMemcpyAsync(bs.host_ctr, bp.ctr, sizeof(BatchCounters), cudaMemcpyDeviceToHost, st));
         for (int32_t r = 0; r < n; ++r)
             TH_CUDA(cudaMemcpyAsync(ctx->batch[r].host, ctx->batch[r].plan.ctr, sizeof(DevCounters),

@@ -829,8 +829,11 @@ void launch_field(const HullPlan& p, cudaStream_t s)
     {
         const int64_t cells = p.level >= 1 ? (int64_t{ 1 } << (3 * (p.level - 1))) : 1;
         const int mgrid = grid_for(cells < p.node_cap ? cells : p.node_cap, 256);
-        cell_masks_kernel<<<mgrid, 256, 0, s>>>(p, true);
-        TH_LAUNCH_CHECK();
+        if (p.own_cell_masks)
+        {
+            cell_masks_kernel<<<mgrid, 256, 0, s>>>(p, true);
+            TH_LAUNCH_CHECK();
+        }
         const int grid = grid_for(p.corner_cap, 32 * kMaskedWarps);
         // at least one launch, so that B == 0 still writes the empty product 1
         for (int64_t b0 = 0; b0 == 0 || b0 < p.B; b0 += 32)
@@ -846,8 +849,11 @@ void launch_field(const HullPlan& p, cudaStream_t s)
                 throw CudaError{ cudaErrorInvalidValue, "hull field: unsupported mask dtype" };
             TH_LAUNCH_CHECK();
         }
-        cell_masks_kernel<<<mgrid, 256, 0, s>>>(p, false);
-        TH_LAUNCH_CHECK();
+        if (p.own_cell_masks)
+        {
+            cell_masks_kernel<<<mgrid, 256, 0, s>>>(p, false);
+            TH_LAUNCH_CHECK();
+        }
         return;
     }
     const int grid = grid_for(p.corner_cap, 256);

@@ -25,6 +25,7 @@ struct BatchReq
     uint64_t* bitmap;
     uint32_t* rowbits;
     int64_t R, WR;
+    uint32_t* cell_masks; // the field's cell-mask table (HullPlan::cell_masks) or nullptr
 };
 
 struct BatchCounters
@@ -64,5 +65,8 @@ void launch_batch_init(const BatchPlan& bp, cudaStream_t s);
 void launch_batch_carve(const BatchPlan& bp, cudaStream_t s);
 // Corner bits of every request's leaves, in one launch.
 void launch_batch_mark(const BatchPlan& bp, cudaStream_t s);
+// The field's cell-mask tables of every request from its level L-1 cells:
+// set before the fields, cleared after them.
+void launch_batch_cell_masks(const BatchPlan& bp, bool set, cudaStream_t s);
 
 } // namespace th

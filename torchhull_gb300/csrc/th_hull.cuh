@@ -96,6 +96,7 @@ struct HullPlan
     // table over the cells of level L-1, scattered before the field and
     // cleared after it (nullptr: no table, every pair is evaluated).
     uint32_t* cell_masks; // [8^(L-1)]
+    bool own_cell_masks;  // launch_field scatters and clears the table (the batched form does it itself)
     // corner grid: R^3 points, one bit each, rows of WR 64-bit words (x fastest)
     int64_t R, WR;
     uint64_t* bitmap;     // [R*R*WR]

@@ -38,8 +38,8 @@ def estimate_bytes(req: HullRequest) -> int:
 
     Mirrors the pool sizing of the C library (csrc/capi.cu: prepare): SAT,
     node and corner pools (capped at 16 M entries, the initial capacity), the
-    all-ones footprint bitmap of the field and the corner bitmap with its
-    rank words.
+    field's all-ones footprint bitmap and cell-mask table, and the corner
+    bitmap with its rank words.
     """
     B, H, W = req.masks.shape[:3]
     inputs = req.masks.numel() * req.masks.element_size() + req.transforms.numel() * req.transforms.element_size()
@@ -51,10 +51,11 @@ def estimate_bytes(req: HullRequest) -> int:
     parents = min(_max_nodes(L), 1 << 22)
     sat = 4 * B * H * W
     ones = 4 * B * H * ((W + 31) // 32)
+    cell_masks = 4 * 8 ** (L - 1) if 1 <= L <= 10 else 0
     node_pool = nodes * (8 + 4 + 4 + 1) + parents * 64
     corner_pool = corners * (8 + 4 + 1 + 1 + 4 + 4)
     bitmap = R * R * WR * (8 + 4) + R * R * 4 + (R * R + 31) // 32 * 4
-    return int(inputs + sat + ones + node_pool + corner_pool + bitmap)
+    return int(inputs + sat + ones + cell_masks + node_pool + corner_pool + bitmap)
 
 
 @dataclasses.dataclass
