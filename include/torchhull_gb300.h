@@ -281,6 +281,12 @@ typedef struct th_stage_times
     float marching_cubes_ms; /* cell codes, edge marks, vertex numbering */
     float total_ms;
     int32_t levels;
+    /* (parent, view) items the carve evaluated per parent level: views skipped
+     * as inherited "object" or out of the frame are not counted */
+    int64_t carve_items[TH_MAX_LEVEL];
+    /* (corner, view) pairs the field evaluated (pairs whose factor the carve
+     * proved to be 1 are not counted) */
+    int64_t field_items;
 } th_stage_times;
 
 th_status th_context_set_profiling(th_context* ctx, int32_t enable);

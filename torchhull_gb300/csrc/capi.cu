@@ -750,6 +750,9 @@ void run_hull_once(th_context* ctx,
         t.field_ms = ev->between(L + 3, L + 4);
         t.marching_cubes_ms = ev->between(L + 4, L + 5);
         t.total_ms = ev->between(0, L + 5);
+        for (int li = 0; li < L; ++li)
+            t.carve_items[li] = static_cast<int64_t>(s.host->items[li]);
+        t.field_items = static_cast<int64_t>(s.host->field_items);
         ctx->times = t;
     }
     if (carve_ms)

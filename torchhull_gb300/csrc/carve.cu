@@ -151,6 +151,9 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_views_kernel
     {
         const int64_t pi = base + grp;
         const bool valid = pi < L.n;
+        if (lane == 0)
+            atomicAdd(&p.ctr->items[li],
+                      static_cast<unsigned long long>(p.B * (L.n - base < G ? L.n - base : G)));
         uint32_t empty = 0, refine = 0, inside = 0, skip = 0, outb = 0;
         if (valid)
         {
@@ -191,7 +194,7 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_views_kernel
         if (valid && sub == 0)
         {
             store_parent(p, L, pi, empty, refine, inside, PARTIAL);
-            if (pi < p.parent_cap)
+            if (pi < p.parent_cap && !L.last)
             {
                 // the children inherit the parent's skip views (all descendants are object there)
                 const uint32_t inherited = produce && L.skips ? L.parent_skip[pi] : 0u;
@@ -249,6 +252,8 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel
         const int incl = warp_inclusive_scan(count);
         const int excl = incl - count;
         const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (lane == 0 && total > 0)
+            atomicAdd(&p.ctr->items[li], static_cast<unsigned long long>(total));
         __syncwarp();
         for (int k0 = 0; k0 < total; k0 += 32)
         {
@@ -315,7 +320,7 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel
         if (valid)
         {
             store_parent(p, L, pi, ws.empty[lane], ws.refine[lane], ws.inside[lane], PARTIAL);
-            if (pi < p.parent_cap)
+            if (pi < p.parent_cap && !L.last)
             {
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
@@ -352,7 +357,8 @@ struct ChildEmit
         const int64_t gx = 2 * (idx & mask), gy = 2 * ((idx >> li) & mask), gz = 2 * (idx >> (2 * li));
         const int sh = li + 1; // children ravel at resolution 2^(li+1)
         const uint32_t m = p.child_masks[i];
-        const bool has_skip = i < p.parent_cap;
+        // the masks of the children of the last level (the leaves) are never read
+        const bool has_skip = i < p.parent_cap && li + 1 < p.level;
         int64_t out = c->level_off[li + 1] + static_cast<int64_t>(off);
 #pragma unroll
         for (int k = 0; k < 8; ++k)

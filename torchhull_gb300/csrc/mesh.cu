@@ -351,6 +351,9 @@ __global__ void __launch_bounds__(256) field_kernel(HullPlan p, int64_t b0, int6
         const float wy = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gy)), inv_rc), length, cy);
         const float wz = __fmaf_rn(__fmul_rn(small_i2f(static_cast<int32_t>(gz)), inv_rc), length, cz);
         float value = b0 == 0 ? 1.f : p.values[t];
+        const unsigned nact = __popc(__activemask());
+        if ((threadIdx.x & 31) == __ffs(__activemask()) - 1)
+            atomicAdd(&p.ctr->field_items, static_cast<unsigned long long>(nact) * nv);
 #pragma unroll 4
         for (int v = 0; v < nv; ++v)
             value = __fmul_rn(value, view_factor<DT, PARTIAL>(p, masks, b0 + v, rows[v], wx, wy, wz, Hf, Wf));
@@ -456,6 +459,9 @@ __global__ void __launch_bounds__(32 * kMaskedWarps) field_masked_kernel(HullPla
         }
         if (!__any_sync(0xffffffffu, skip != 0))
         {
+            const unsigned nvalid = __popc(__ballot_sync(0xffffffffu, valid));
+            if (lane == 0)
+                atomicAdd(&p.ctr->field_items, static_cast<unsigned long long>(nvalid) * nv);
             if (valid)
             {
 #pragma unroll 4
@@ -470,6 +476,8 @@ __global__ void __launch_bounds__(32 * kMaskedWarps) field_masked_kernel(HullPla
         const int incl = warp_inclusive_scan(count);
         const int excl = incl - count;
         const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (lane == 0 && total > 0)
+            atomicAdd(&p.ctr->field_items, static_cast<unsigned long long>(total));
         for (int k0 = 0; k0 < total; k0 += 32)
         {
             const int k = k0 + lane;

@@ -29,6 +29,8 @@ struct DevCounters
     int64_t verts;                      // unique mesh vertices
     int64_t overflow;                   // OverflowBits
     int64_t row_words;                  // words of the row-occupancy bitmap
+    unsigned long long items[kMaxLevel];  // (parent, view) items the carve evaluated per parent level
+    unsigned long long field_items;       // (corner, view) pairs the field evaluated
     ScanState scan;
 };
 

@@ -453,6 +453,11 @@ pybind11::dict stage_times(int device)
     for (int i = 0; i < t.levels; ++i)
         carve.append(t.carve_ms[i]);
     d["carve"] = carve;
+    pybind11::list items;
+    for (int i = 0; i < t.levels; ++i)
+        items.append(t.carve_items[i]);
+    d["carve_items"] = items;
+    d["field_items"] = t.field_items;
     d["corners"] = t.corners_ms;
     d["field"] = t.field_ms;
     d["marching_cubes"] = t.marching_cubes_ms;
