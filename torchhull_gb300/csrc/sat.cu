@@ -10,8 +10,8 @@
 //
 // Column pass: one thread per (view, column) walks down the column; a warp
 // covers 32 adjacent columns, so each step is one coalesced 128-byte row read.
-// Row pass: one warp per 32 rows walks across them through a 32x33 shared
-// tile (coalesced loads and stores, one lane per row scanning its 32 values).
+// Row pass: one warp per 32 rows walks across them through 32x33 shared
+// tiles (coalesced loads and stores, one lane per row scanning its 32 values).
 // HBM traffic: read masks + write columns + read columns + write SAT.
 
 #include "th_common.cuh"
@@ -44,12 +44,25 @@ __global__ void __launch_bounds__(256) sat_columns_kernel(const void* __restrict
     float acc = 0.f;
     bool nb = false;
     int64_t y = 0;
-    for (; y + kColUnroll <= H; y += kColUnroll)
+    // two chunks of rows in flight: the next chunk's loads are issued before
+    // the current one is summed (a thread walks its column sequentially)
+    const int64_t full = H - H % kColUnroll;
+    float v[kColUnroll];
+    if (full > 0)
     {
-        float v[kColUnroll];
 #pragma unroll
         for (int k = 0; k < kColUnroll; ++k)
-            v[k] = load_f32<DT>(masks, base + (y + k) * W);
+            v[k] = load_f32<DT>(masks, base + k * W);
+    }
+    for (; y < full; y += kColUnroll)
+    {
+        float nx[kColUnroll];
+        if (y + kColUnroll < full)
+        {
+#pragma unroll
+            for (int k = 0; k < kColUnroll; ++k)
+                nx[k] = load_f32<DT>(masks, base + (y + kColUnroll + k) * W);
+        }
 #pragma unroll
         for (int k = 0; k < kColUnroll; ++k)
         {
@@ -57,6 +70,9 @@ __global__ void __launch_bounds__(256) sat_columns_kernel(const void* __restrict
             acc = __fadd_rn(acc, v[k]);
             out[base + (y + k) * W] = acc;
         }
+#pragma unroll
+        for (int k = 0; k < kColUnroll; ++k)
+            v[k] = nx[k];
     }
     for (; y < H; ++y)
     {
@@ -69,37 +85,50 @@ __global__ void __launch_bounds__(256) sat_columns_kernel(const void* __restrict
         atomicOr(nonbinary, 1u);
 }
 
-__global__ void __launch_bounds__(256) sat_rows_kernel(float* __restrict__ data, int64_t rows, int64_t W)
+constexpr int kRowWarps = 4;
+
+// Row pass: a warp owns 32 rows and walks across them in 32-column tiles
+// through shared memory; the next tile is loaded while the current one is
+// scanned (double buffer).
+__global__ void __launch_bounds__(32 * kRowWarps) sat_rows_kernel(float* __restrict__ data, int64_t rows, int64_t W)
 {
-    __shared__ float tile[8][32][33];
+    __shared__ float tile[kRowWarps][2][32][33];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t row0 = (static_cast<int64_t>(blockIdx.x) * 8 + warp) * 32;
+    const int64_t row0 = (static_cast<int64_t>(blockIdx.x) * kRowWarps + warp) * 32;
     if (row0 >= rows)
         return;
     const int nrows = static_cast<int>(rows - row0 < 32 ? rows - row0 : 32);
-    float (*t)[33] = tile[warp];
-    float carry = 0.f;
-    for (int64_t x0 = 0; x0 < W; x0 += 32)
-    {
+    float(*t)[32][33] = tile[warp];
+    auto load = [&](int buf, int64_t x0) {
         const int64_t x = x0 + lane;
         const bool xin = x < W;
         for (int r = 0; r < nrows; ++r)
-            t[r][lane] = xin ? data[(row0 + r) * W + x] : 0.f;
+            t[buf][r][lane] = xin ? data[(row0 + r) * W + x] : 0.f;
+    };
+    load(0, 0);
+    float carry = 0.f;
+    int buf = 0;
+    for (int64_t x0 = 0; x0 < W; x0 += 32)
+    {
+        if (x0 + 32 < W)
+            load(buf ^ 1, x0 + 32);
         __syncwarp();
         if (lane < nrows)
         {
             const int cnt = static_cast<int>(W - x0 < 32 ? W - x0 : 32);
             for (int c = 0; c < cnt; ++c)
             {
-                carry = __fadd_rn(carry, t[lane][c]);
-                t[lane][c] = carry;
+                carry = __fadd_rn(carry, t[buf][lane][c]);
+                t[buf][lane][c] = carry;
             }
         }
         __syncwarp();
+        const int64_t x = x0 + lane;
         for (int r = 0; r < nrows; ++r)
-            if (xin)
-                data[(row0 + r) * W + x] = t[r][lane];
+            if (x < W)
+                data[(row0 + r) * W + x] = t[buf][r][lane];
         __syncwarp();
+        buf ^= 1;
     }
 }
 
@@ -133,8 +162,8 @@ void launch_integral_image(const void* masks,
         throw CudaError{ cudaErrorInvalidValue, "integral image: unsupported mask dtype" };
     TH_LAUNCH_CHECK();
     const int64_t rows = B * H;
-    const unsigned grid_rows = static_cast<unsigned>((rows + 255) / 256);
-    sat_rows_kernel<<<grid_rows, 256, 0, s>>>(out, rows, W);
+    const unsigned grid_rows = static_cast<unsigned>((rows + 32 * kRowWarps - 1) / (32 * kRowWarps));
+    sat_rows_kernel<<<grid_rows, 32 * kRowWarps, 0, s>>>(out, rows, W);
     TH_LAUNCH_CHECK();
 }
 
