@@ -1428,6 +1428,9 @@ th_status th_visual_hull_export_candidates(th_context* ctx, int32_t level, int64
         {
             if (!dst)
                 throw ArgError{ TH_ERR_INVALID_ARGUMENT, "dst is NULL" };
+            // the leaves are written out on demand
+            if (level == s.plan.level)
+                launch_emit_leaves(s.plan, static_cast<cudaStream_t>(stream));
             TH_CUDA(cudaMemcpyAsync(dst, s.plan.nodes + s.host->level_off[level], sizeof(int64_t) * n,
                                     cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)));
         }

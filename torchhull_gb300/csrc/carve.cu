@@ -456,8 +456,29 @@ void launch_carve_level(const HullPlan& p, int li, cudaStream_t s)
             launch_classify<false, false>(p, li, max_parents, s);
     }
     TH_LAUNCH_CHECK();
+    if (li + 1 == p.level)
+    {
+        // The leaves are not written out: their corners are marked from the
+        // parents' child masks (launch_corners), and the leaf list is emitted
+        // only when the candidates of the last level are exported.  The count
+        // (and the pool check) is still taken here.
+        run_scan_reduce(ChildCount{ p.child_masks }, ChildEpilogue{ p.ctr, li, p.node_cap, p.parent_cap },
+                        Count{ &p.ctr->level_count[li], 0 }, max_parents, p.tile_sums, &p.ctr->scan, s);
+        return;
+    }
     run_scan(ChildCount{ p.child_masks }, ChildEmit{ p, li }, ChildEpilogue{ p.ctr, li, p.node_cap, p.parent_cap },
              Count{ &p.ctr->level_count[li], 0 }, max_parents, p.tile_sums, &p.ctr->scan, s);
+}
+
+void launch_emit_leaves(const HullPlan& p, cudaStream_t s)
+{
+    const int li = p.level - 1;
+    if (li < 0)
+        return;
+    const int64_t bound = li < 10 ? (int64_t{ 1 } << (3 * li)) : p.node_cap;
+    const int64_t max_parents = bound < p.node_cap ? bound : p.node_cap;
+    run_scan(ChildCount{ p.child_masks }, ChildEmit{ p, li }, NoEpilogue{}, Count{ &p.ctr->level_count[li], 0 },
+             max_parents, p.tile_sums, &p.ctr->scan, s);
 }
 
 } // namespace th

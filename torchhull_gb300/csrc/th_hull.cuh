@@ -136,6 +136,9 @@ void launch_hull_init(const HullPlan& p, cudaStream_t s);
 // Sparse field export: ravelled ids (x + y*R + z*R*R) and values.
 void launch_export_field(const HullPlan& p, int64_t n, int64_t* indices, float* values, cudaStream_t s);
 void launch_carve_level(const HullPlan& p, int level_index, cudaStream_t s);
+// The leaf list (level L) from the last level's child masks; the carve itself
+// only counts the leaves.
+void launch_emit_leaves(const HullPlan& p, cudaStream_t s);
 void launch_corners(const HullPlan& p, cudaStream_t s);
 // The part of launch_corners after the bitmap is set: touched rows, sorted
 // unique corners and per-word ranks.
