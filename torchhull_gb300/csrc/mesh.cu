@@ -72,15 +72,36 @@ __global__ void __launch_bounds__(256) mark_corners_kernel(HullPlan p)
 {
     const DevCounters* c = p.ctr;
     const int L = p.level;
-    const int64_t n = c->level_count[L];
-    const int64_t* leaves = p.nodes + c->level_off[L];
-    const int64_t r = int64_t{ 1 } << L;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
+    const int64_t t0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (L == 0)
     {
-        const int64_t idx = leaves[t];
-        const int64_t x = idx & (r - 1), y = (idx >> L) & (r - 1), z = idx >> (2 * L);
-        mark_cell_corners(p.bitmap, p.rowbits, p.R, p.WR, x, y, z);
+        // the root is the only leaf
+        if (t0 == 0 && c->level_count[0] > 0)
+            mark_cell_corners(p.bitmap, p.rowbits, p.R, p.WR, 0, 0, 0);
+        return;
+    }
+    // the leaves are the refined children of the level L-1 cells (their
+    // child masks), which the carve does not write out
+    if (c->level_count[L] == 0)
+        return;
+    const int li = L - 1;
+    const int64_t n = c->level_count[li];
+    const int64_t* parents = p.nodes + c->level_off[li];
+    const int64_t r = int64_t{ 1 } << li;
+    for (int64_t t = t0; t < n; t += stride)
+    {
+        uint32_t m = p.child_masks[t];
+        if (!m)
+            continue;
+        const int64_t idx = parents[t];
+        const int64_t x = 2 * (idx & (r - 1)), y = 2 * ((idx >> li) & (r - 1)), z = 2 * (idx >> (2 * li));
+        while (m)
+        {
+            const int k = __ffs(m) - 1;
+            m &= m - 1;
+            mark_cell_corners(p.bitmap, p.rowbits, p.R, p.WR, x + (k & 1), y + (k >> 1 & 1), z + (k >> 2 & 1));
+        }
     }
 }
 
@@ -374,16 +395,37 @@ __global__ void __launch_bounds__(256) cell_masks_kernel(HullPlan p, bool set)
         p.cell_masks[p.nodes[off + k]] = set ? (p.node_skip[off + k] | p.node_out[off + k]) : 0u;
 }
 
-// Views of a corner whose field factor is exactly 1: the cell-mask entry of
-// the level L-1 cell (x >> 1, y >> 1, z >> 1), whose lattice holds the corner
-// (0 when the corner lies on the far faces of the grid).
+// Views of a corner whose field factor is exactly 1: the OR of the cell-mask
+// entries of the level L-1 cells whose lattice holds the corner (x >> 1, and
+// also (x - 1) >> 1 for an even x > 0, per axis; cells beyond the grid and
+// cells that are no node hold 0).
 __device__ __forceinline__ uint32_t corner_view_mask(const HullPlan& p, int64_t gx, int64_t gy, int64_t gz)
 {
     const int li = p.level - 1;
-    const int64_t cx = gx >> 1, cy = gy >> 1, cz = gz >> 1, r = int64_t{ 1 } << li;
-    if (cx >= r || cy >= r || cz >= r)
-        return 0u;
-    return p.cell_masks[cx | (cy << li) | (cz << (2 * li))];
+    const int64_t r = int64_t{ 1 } << li;
+    const int64_t x0 = gx >> 1, y0 = gy >> 1, z0 = gz >> 1;
+    const int64_t x1 = (gx - 1) >> 1, y1 = (gy - 1) >> 1, z1 = (gz - 1) >> 1;
+    const int nx = (x1 != x0 && gx > 0) ? 2 : 1, ny = (y1 != y0 && gy > 0) ? 2 : 1, nz = (z1 != z0 && gz > 0) ? 2 : 1;
+    uint32_t m = 0;
+    for (int k = 0; k < nz; ++k)
+    {
+        const int64_t cz = k ? z1 : z0;
+        if (cz >= r)
+            continue;
+        for (int j = 0; j < ny; ++j)
+        {
+            const int64_t cy = j ? y1 : y0;
+            if (cy >= r)
+                continue;
+            for (int i = 0; i < nx; ++i)
+            {
+                const int64_t cx = i ? x1 : x0;
+                if (cx < r)
+                    m |= p.cell_masks[cx | (cy << li) | (cz << (2 * li))];
+            }
+        }
+    }
+    return m;
 }
 
 // Position of the set bit of m with j set bits below it (j < popc(m)).
