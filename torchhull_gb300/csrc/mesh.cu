@@ -153,34 +153,97 @@ struct CornerCount
     }
 };
 
-struct CornerEmit
+
+// Position of the set bit of the 64-bit word w with j set bits below it.
+__device__ __forceinline__ int nth_set_bit64(uint64_t w, int j)
 {
-    HullPlan p;
-    __device__ void operator()(int64_t k, unsigned long long off, unsigned long long) const
+    const uint32_t lo = static_cast<uint32_t>(w);
+    const int c = __popc(lo);
+    return j < c ? nth_set_bit(lo, j) : 32 + nth_set_bit(static_cast<uint32_t>(w >> 32), j - c);
+}
+
+// Pass 2 of the corner scan (the counts come from CornerCount's tile sums):
+// a block owns one scan tile of kScanTile words, a warp 8 chunks of 32
+// consecutive words.  Per chunk the warp numbers the words' corners by a
+// warp scan and writes them with all lanes: corner k of the chunk belongs to
+// the word whose offset is the last one <= k, so the stores are coalesced.
+// Also stores each word's rank (word_rank).
+__global__ void __launch_bounds__(kScanThreads) corner_emit_kernel(HullPlan p, const unsigned long long* __restrict__ tile_offsets)
+{
+    static_assert(kScanThreads == 256 && kScanItems == 8, "one warp chunk per 32 items");
+    __shared__ unsigned long long warp_totals[kScanThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t n = p.ctr->rows * p.WR;
+    const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+    const uint32_t wr = static_cast<uint32_t>(p.WR), R = static_cast<uint32_t>(p.R);
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
     {
-        const uint32_t wr = static_cast<uint32_t>(p.WR), kk = static_cast<uint32_t>(k);
-        const uint32_t row = p.rows[kk / wr], wi = kk % wr;
-        const int64_t w = static_cast<int64_t>(row) * p.WR + wi;
-        uint64_t word = p.bitmap[w];
-        p.word_rank[w] = static_cast<uint32_t>(off);
-        if (!word)
-            return;
-        const uint32_t ry = row % static_cast<uint32_t>(p.R);
-        const uint32_t rz = row / static_cast<uint32_t>(p.R);
-        uint64_t out = off;
-        while (word)
+        const int64_t first = tile * kScanTile + static_cast<int64_t>(w) * 256;
+        uint64_t words[8];
+        unsigned long long wsum = 0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
         {
-            const int bit = __ffsll(static_cast<long long>(word)) - 1;
-            if (static_cast<int64_t>(out) < p.corner_cap)
+            const int64_t k = first + c * 32 + lane;
+            words[c] = 0;
+            if (k < n)
             {
-                p.corners[out] = pack_corner(static_cast<int64_t>(wi) * 64 + bit, ry, rz);
-                p.emask[out] = 0;
+                const uint32_t kk = static_cast<uint32_t>(k);
+                words[c] = p.bitmap[static_cast<int64_t>(p.rows[kk / wr]) * p.WR + kk % wr];
             }
-            ++out;
-            word &= word - 1;
+            wsum += __popcll(words[c]);
+        }
+        // this warp's corners come after those of the tile's earlier warps
+        unsigned long long wtot = wsum;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1)
+            wtot += __shfl_xor_sync(0xffffffffu, wtot, d);
+        if (lane == 0)
+            warp_totals[w] = wtot;
+        __syncthreads();
+        unsigned long long running = tile_offsets[tile];
+        for (int v = 0; v < w; ++v)
+            running += warp_totals[v];
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+        {
+            const int64_t k = first + c * 32 + lane;
+            const int cnt = __popcll(words[c]);
+            const int incl = warp_inclusive_scan(cnt);
+            const int excl = incl - cnt;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            uint32_t row = 0, wi = 0;
+            if (k < n)
+            {
+                const uint32_t kk = static_cast<uint32_t>(k);
+                row = p.rows[kk / wr];
+                wi = kk % wr;
+                p.word_rank[static_cast<int64_t>(row) * p.WR + wi] = static_cast<uint32_t>(running + excl);
+            }
+            for (int k0 = 0; k0 < total; k0 += 32)
+            {
+                const int kk = k0 + lane;
+                const int s = item_slot(excl, kk);
+                const int es = __shfl_sync(0xffffffffu, excl, s);
+                const uint64_t ws = __shfl_sync(0xffffffffu, words[c], s);
+                const uint32_t rs = __shfl_sync(0xffffffffu, row, s);
+                const uint32_t wis = __shfl_sync(0xffffffffu, wi, s);
+                if (kk < total)
+                {
+                    const int bit = nth_set_bit64(ws, kk - es);
+                    const int64_t out = static_cast<int64_t>(running) + kk;
+                    if (out < p.corner_cap)
+                    {
+                        p.corners[out] = pack_corner(static_cast<int64_t>(wis) * 64 + bit, rs % R, rs / R);
+                        p.emask[out] = 0;
+                    }
+                }
+            }
+            running += static_cast<unsigned long long>(total);
         }
     }
-};
+}
 
 struct CornerEpilogue
 {
@@ -426,27 +489,6 @@ __device__ __forceinline__ uint32_t corner_view_mask(const HullPlan& p, int64_t 
         }
     }
     return m;
-}
-
-// Position of the set bit of m with j set bits below it (j < popc(m)).
-__device__ __forceinline__ int nth_set_bit(uint32_t m, int j)
-{
-    int pos = 0;
-#pragma unroll
-    for (int w = 16; w > 0; w >>= 1)
-    {
-        const uint32_t low = m & ((1u << w) - 1u);
-        const int c = __popc(low);
-        if (j >= c)
-        {
-            j -= c;
-            pos += w;
-            m >>= w;
-        }
-        else
-            m = low;
-    }
-    return pos;
 }
 
 constexpr int kMaskedWarps = 8;
@@ -729,8 +771,11 @@ __global__ void __launch_bounds__(256) export_verts_kernel(HullPlan p, float* __
         {
             if (!(bits >> a & 1u))
                 continue;
-            uint32_t r2 = 0;
-            corner_rank(p, gx + (a == 0), gy + (a == 1), gz + (a == 2), r2);
+            // a vertex edge joins two corners of a cell; the +x neighbour of a
+            // set point is the next one in the bitmap's order
+            uint32_t r2 = static_cast<uint32_t>(t + 1);
+            if (a > 0)
+                corner_rank(p, gx, gy + (a == 1), gz + (a == 2), r2);
             float v[3];
             edge_vertex(p, gx, gy, gz, a, v1, p.values[r2], scale, v);
             verts[3 * out + 0] = v[0];
@@ -859,8 +904,11 @@ void launch_rank_corners(const HullPlan& p, cudaStream_t s)
     const int64_t row_words = (p.R * p.R + 31) / 32;
     run_scan(RowCount{ p.rowbits }, RowEmit{ p.rowbits, p.rows }, RowEpilogue{ p.ctr }, Count{ nullptr, row_words },
              row_words, p.tile_sums, &p.ctr->scan, s);
-    run_scan(CornerCount{ p }, CornerEmit{ p }, CornerEpilogue{ p.ctr, p.corner_cap }, Count{ &p.ctr->rows, 0, p.WR },
-             p.R * p.R * p.WR, p.tile_sums, &p.ctr->scan, s);
+    const int64_t max_words = p.R * p.R * p.WR;
+    run_scan_reduce(CornerCount{ p }, CornerEpilogue{ p.ctr, p.corner_cap }, Count{ &p.ctr->rows, 0, p.WR }, max_words,
+                    p.tile_sums, &p.ctr->scan, s);
+    corner_emit_kernel<<<scan_grid(max_words), kScanThreads, 0, s>>>(p, p.tile_sums);
+    TH_LAUNCH_CHECK();
 }
 
 void launch_field(const HullPlan& p, cudaStream_t s)

@@ -266,6 +266,27 @@ __device__ __forceinline__ int item_slot(int excl, int k)
     return s;
 }
 
+// Position of the set bit of m with j set bits below it (j < popc(m)).
+__device__ __forceinline__ int nth_set_bit(uint32_t m, int j)
+{
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w > 0; w >>= 1)
+    {
+        const uint32_t low = m & ((1u << w) - 1u);
+        const int c = __popc(low);
+        if (j >= c)
+        {
+            j -= c;
+            pos += w;
+            m >>= w;
+        }
+        else
+            m = low;
+    }
+    return pos;
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_inclusive_scan(T v)
 {
