@@ -416,33 +416,49 @@ __global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(CountF count,
 }
 
 // emit(i, exclusive_offset, count) is called for every item (count may be 0).
+// A warp takes kScanItems chunks of 32 consecutive items, one item per lane,
+// so that the counts' loads and the emits' stores of a chunk are coalesced;
+// a warp scan per chunk and the warps' totals give the offsets.
 template <class CountF, class EmitF>
 __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(CountF count,
                                                                   EmitF emit,
                                                                   Count n_src,
                                                                   const unsigned long long* __restrict__ tile_offsets)
 {
+    __shared__ unsigned long long warp_tot[kScanThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t n = n_src.get();
     const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
     {
-        const int64_t base = tile * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
+        const int64_t first = tile * kScanTile + static_cast<int64_t>(w) * (32 * kScanItems);
         unsigned long long c[kScanItems];
         unsigned long long s = 0;
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k)
         {
-            c[k] = (base + k < n) ? count(base + k) : 0ull;
+            const int64_t i = first + k * 32 + lane;
+            c[k] = (i < n) ? count(i) : 0ull;
             s += c[k];
         }
-        unsigned long long tot;
-        unsigned long long off = block_exclusive_scan(s, &tot) + tile_offsets[tile];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1)
+            s += __shfl_xor_sync(0xffffffffu, s, d);
+        if (lane == 0)
+            warp_tot[w] = s;
+        __syncthreads();
+        unsigned long long off = tile_offsets[tile];
+        for (int v = 0; v < w; ++v)
+            off += warp_tot[v];
+        __syncthreads();
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k)
         {
-            if (base + k < n)
-                emit(base + k, off, c[k]);
-            off += c[k];
+            const unsigned long long incl = warp_inclusive_scan(c[k]);
+            const int64_t i = first + k * 32 + lane;
+            if (i < n)
+                emit(i, off + incl - c[k], c[k]);
+            off += __shfl_sync(0xffffffffu, incl, 31);
         }
     }
 }
