@@ -296,20 +296,24 @@ __global__ void __launch_bounds__(256) batch_mark_kernel(BatchPlan bp)
         starts[li] = s;
         s += level_entries(bp, li, s);
     }
-    const int64_t total = s;
+    starts[bp.max_level + 1] = s;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride)
+    // only the lists of the levels some request ends at
+    for (int li = 0; li <= bp.max_level; ++li)
     {
-        int li = 0;
-        while (li < bp.max_level && starts[li + 1] <= t)
-            ++li;
-        const int64_t node = bp.nodes[t];
-        const BatchReq& q = bp.reqs[static_cast<int>(node >> kTagShift)];
-        if (q.level != li)
+        if (!((bp.leaf_levels >> li) & 1u))
             continue;
-        const int64_t cell = node & kCellMask;
         const int64_t m = (int64_t{ 1 } << li) - 1;
-        mark_cell_corners(q.bitmap, q.rowbits, q.R, q.WR, cell & m, (cell >> li) & m, cell >> (2 * li));
+        for (int64_t t = starts[li] + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < starts[li + 1];
+             t += stride)
+        {
+            const int64_t node = bp.nodes[t];
+            const BatchReq& q = bp.reqs[static_cast<int>(node >> kTagShift)];
+            if (q.level != li)
+                continue;
+            const int64_t cell = node & kCellMask;
+            mark_cell_corners(q.bitmap, q.rowbits, q.R, q.WR, cell & m, (cell >> li) & m, cell >> (2 * li));
+        }
     }
 }
 
@@ -324,17 +328,21 @@ __global__ void __launch_bounds__(256) batch_cell_masks_kernel(BatchPlan bp, boo
         starts[li] = s;
         s += level_entries(bp, li, s);
     }
-    const int64_t total = s;
+    starts[bp.max_level + 1] = s;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride)
+    // only the lists of the levels L-1 of requests with a table
+    for (int li = 0; li <= bp.max_level; ++li)
     {
-        int li = 0;
-        while (li < bp.max_level && starts[li + 1] <= t)
-            ++li;
-        const int64_t node = bp.nodes[t];
-        const BatchReq& q = bp.reqs[static_cast<int>(node >> kTagShift)];
-        if (q.cell_masks && li == q.level - 1)
-            q.cell_masks[node & kCellMask] = set ? (bp.node_skip[t] | bp.node_out[t]) : 0u;
+        if (!((bp.mask_levels >> li) & 1u))
+            continue;
+        for (int64_t t = starts[li] + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < starts[li + 1];
+             t += stride)
+        {
+            const int64_t node = bp.nodes[t];
+            const BatchReq& q = bp.reqs[static_cast<int>(node >> kTagShift)];
+            if (q.cell_masks && li == q.level - 1)
+                q.cell_masks[node & kCellMask] = set ? (bp.node_skip[t] | bp.node_out[t]) : 0u;
+        }
     }
 }
 

@@ -908,6 +908,15 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
         bp.child_out = bs.child_out.as<uint32_t>();
         bp.skip_cap = skip_cap;
         bp.block_sums = bs.block_sums.as<unsigned long long>();
+        bp.leaf_levels = 0;
+        bp.mask_levels = 0;
+        for (int32_t r = 0; r < n; ++r)
+        {
+            const BatchReq& q = bs.host_reqs[r];
+            bp.leaf_levels |= 1u << q.level;
+            if (q.cell_masks && q.level >= 1)
+                bp.mask_levels |= 1u << (q.level - 1);
+        }
         bp.variant = -1;
         for (int32_t r = 0; r < n; ++r)
         {

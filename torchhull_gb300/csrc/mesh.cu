@@ -751,41 +751,6 @@ __device__ __forceinline__ void edge_vertex(const HullPlan& p,
         out[a] = __fmaf_rn(scale, q[a], p.corner[a]);
 }
 
-__global__ void __launch_bounds__(256) export_verts_kernel(HullPlan p, float* __restrict__ verts)
-{
-    const int64_t n = p.ctr->corners;
-    const float scale = __fdiv_rn(p.length, static_cast<float>(int64_t{ 1 } << p.level));
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride)
-    {
-        const uint32_t bits = p.emask[t];
-        if (!bits)
-            continue;
-        const int64_t idx = p.corners[t];
-        int64_t gx, gy, gz;
-        unpack_corner(idx, gx, gy, gz);
-        const float v1 = p.values[t];
-        int64_t out = p.vbase[t];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-        {
-            if (!(bits >> a & 1u))
-                continue;
-            // a vertex edge joins two corners of a cell; the +x neighbour of a
-            // set point is the next one in the bitmap's order
-            uint32_t r2 = static_cast<uint32_t>(t + 1);
-            if (a > 0)
-                corner_rank(p, gx, gy + (a == 1), gz + (a == 2), r2);
-            float v[3];
-            edge_vertex(p, gx, gy, gz, a, v1, p.values[r2], scale, v);
-            verts[3 * out + 0] = v[0];
-            verts[3 * out + 1] = v[1];
-            verts[3 * out + 2] = v[2];
-            ++out;
-        }
-    }
-}
-
 // Faces in soup order; with unique vertices they index the edge-numbered
 // vertex list, without they index the soup, which this kernel also writes.
 // Columns 1 and 2 are swapped as flip_faces does (visual_hull_cuda.cu:941-956).
@@ -868,6 +833,109 @@ __global__ void __launch_bounds__(32 * kExportWarps) export_faces_kernel(HullPla
                     verts[3 * f + 2] = v[2];
                     stage[dst] = f;
                 }
+            }
+        }
+        __syncwarp();
+        for (int i = lane; i < total; i += 32)
+            faces[lo + i] = stage[i];
+        __syncwarp();
+    }
+}
+
+// Unique vertices: vertices and faces in one pass.  A warp takes 32
+// consecutive corners; their vertices (one per set edge bit, numbered by
+// vbase) and their cells' face entries (numbered by soup_off) are two
+// contiguous output ranges, each dealt out one entry per lane and stored
+// coalesced.  The +x neighbour of a vertex edge is the next corner rank; the
+// faces look their corners' ranks up once per cell (cell_ranks).
+__global__ void __launch_bounds__(32 * kExportWarps) export_mesh_kernel(HullPlan p, float* __restrict__ verts, int64_t* __restrict__ faces)
+{
+    __shared__ TableCache tab;
+    __shared__ int64_t stage_all[kExportWarps][32 * 15];
+    __shared__ uint32_t ranks_all[kExportWarps][32][9];
+    load_tables(tab);
+    int64_t* stage = stage_all[threadIdx.x >> 5];
+    uint32_t(*ranks)[9] = ranks_all[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int64_t n = p.ctr->corners;
+    const float scale = __fdiv_rn(p.length, static_cast<float>(int64_t{ 1 } << p.level));
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t wb = warp * 32; wb < n; wb += nwarps * 32)
+    {
+        const int64_t t = wb + lane;
+        const bool valid = t < n;
+        const uint32_t code = valid ? p.codes[t] : 0u;
+        const int cnt = tab.count[code];
+        const uint32_t bits = valid ? p.emask[t] : 0u;
+        const int nvert = __popc(bits);
+        if (!__any_sync(0xffffffffu, cnt > 0 || nvert > 0))
+            continue;
+        const int64_t id = (cnt > 0 || nvert > 0) ? p.corners[t] : 0;
+
+        // vertices: the warp's range starts at lane 0's vertex base
+        const int64_t vlo = __shfl_sync(0xffffffffu, valid ? static_cast<int64_t>(p.vbase[t]) : int64_t{ 0 }, 0);
+        const float v1 = nvert ? p.values[t] : 0.f;
+        const int vincl = warp_inclusive_scan(nvert);
+        const int vexcl = vincl - nvert;
+        const int vtot = __shfl_sync(0xffffffffu, vincl, 31);
+        for (int k0 = 0; k0 < vtot; k0 += 32)
+        {
+            const int k = k0 + lane;
+            const int s = item_slot(vexcl, k);
+            const int es = __shfl_sync(0xffffffffu, vexcl, s);
+            const uint32_t bs = __shfl_sync(0xffffffffu, bits, s);
+            const int64_t ids = __shfl_sync(0xffffffffu, id, s);
+            const float v1s = __shfl_sync(0xffffffffu, v1, s);
+            if (k < vtot)
+            {
+                const int a = nth_set_bit(bs, k - es);
+                int64_t gx, gy, gz;
+                unpack_corner(ids, gx, gy, gz);
+                uint32_t r2 = static_cast<uint32_t>(wb + s + 1);
+                if (a > 0)
+                    corner_rank(p, gx, gy + (a == 1), gz + (a == 2), r2);
+                float v[3];
+                edge_vertex(p, gx, gy, gz, a, v1s, p.values[r2], scale, v);
+                const int64_t out = vlo + k;
+                verts[3 * out + 0] = v[0];
+                verts[3 * out + 1] = v[1];
+                verts[3 * out + 2] = v[2];
+            }
+        }
+
+        // faces
+        if (!__any_sync(0xffffffffu, cnt > 0))
+            continue;
+        const int64_t lo = __shfl_sync(0xffffffffu, valid ? static_cast<int64_t>(p.soup_off[t]) : int64_t{ 0 }, 0);
+        if (cnt > 0)
+        {
+            int64_t gx, gy, gz;
+            unpack_corner(id, gx, gy, gz);
+            uint32_t rk[8];
+            cell_ranks(p, t, n, gx, gy, gz, rk);
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                ranks[lane][i] = rk[i];
+        }
+        const int incl = warp_inclusive_scan(cnt);
+        const int excl = incl - cnt;
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        for (int k0 = 0; k0 < total; k0 += 32)
+        {
+            const int k = k0 + lane;
+            const int s = item_slot(excl, k);
+            const int es = __shfl_sync(0xffffffffu, excl, s);
+            const uint32_t cs = __shfl_sync(0xffffffffu, code, s);
+            if (k < total)
+            {
+                const uint32_t e = tab.edges[cs][k - es];
+                const int lo_corner = static_cast<int>(e & 7u), axis = static_cast<int>(e >> 3);
+                const int slot = k % 3; // lo is a multiple of 3
+                const int dst = k - slot + (slot == 0 ? 0 : 3 - slot);
+                const uint32_t r1 = ranks[s][lo_corner];
+                stage[dst] = static_cast<int64_t>(p.vbase[r1]) + __popc(p.emask[r1] & ((1u << axis) - 1u));
             }
         }
         __syncwarp();
@@ -981,13 +1049,11 @@ void launch_marching_cubes(const HullPlan& p, cudaStream_t s)
 
 void launch_export(const HullPlan& p, float* verts, int64_t* faces, cudaStream_t s)
 {
-    const int grid = grid_for(p.corner_cap, 256);
+    const int grid = grid_for(p.corner_cap, 32 * kExportWarps);
     if (p.unique)
-    {
-        export_verts_kernel<<<grid, 256, 0, s>>>(p, verts);
-        TH_LAUNCH_CHECK();
-    }
-    export_faces_kernel<<<grid_for(p.corner_cap, 32 * kExportWarps), 32 * kExportWarps, 0, s>>>(p, verts, faces);
+        export_mesh_kernel<<<grid, 32 * kExportWarps, 0, s>>>(p, verts, faces);
+    else
+        export_faces_kernel<<<grid, 32 * kExportWarps, 0, s>>>(p, verts, faces);
     TH_LAUNCH_CHECK();
 }
 

@@ -58,6 +58,8 @@ struct BatchPlan
     uint32_t* child_out;   // [skip_cap * 8]
     int64_t skip_cap;
     unsigned long long* block_sums; // [grid size] children per block
+    uint32_t leaf_levels; // bit i: some request ends at level i
+    uint32_t mask_levels; // bit i: some request with a cell-mask table has level i + 1
 };
 
 void launch_batch_init(const BatchPlan& bp, cudaStream_t s);
