@@ -310,6 +310,7 @@ def run_gb300(args) -> dict | None:
     th._C.set_carve_kernel(local, {"auto": 0, "views": 1, "items": 2}[args.carve_kernel])
     th._C.set_batch_route(local, args.batch_route == "on")
     th._C.set_field_ones(local, args.field_ones == "on")
+    th._C.set_field_masks(local, args.field_masks == "on")
 
     if args.mode == "hetero":
         return finish(run_hetero(args, th, scenes, dev, world, rank), world)
@@ -413,7 +414,7 @@ def run_gb300(args) -> dict | None:
         "config": {"workload": WORKLOAD, "requests_per_step": Q, "level": LEVEL, "views": VIEWS, "side": SIDE,
                    "l2": "inputs larger than L2 (128 MiB of masks + 128 MiB SAT per request)",
                    "path": "batched form (th_visual_hull_batch: one persistent carve launch per step)",
-                   "field_ones": args.field_ones,
+                   "field_ones": args.field_ones, "field_masks": args.field_masks,
                    "mesh_verts": nv, "mesh_faces": nf, "leaves": levels[-1], "corners": corners},
         "plain": {"value": plain_value, "unit": "hulls/s", "p50_ms": percentile(per_hull, 50),
                   "p99_ms": percentile(per_hull, 99), "path": "torchhull_gb300.visual_hull, one request per call"},
@@ -716,7 +717,9 @@ def main() -> None:
     ap.add_argument("--batch-route", choices=["on", "off"], default="off",
                     help="batched form: requests that fill the GPU alone through the per-request pipeline")
     ap.add_argument("--field-ones", choices=["on", "off"], default="on",
-                    help="field: test a bitmap of all-ones 2x2 pixel footprints before sampling the masks")
+                    help="field without cell masks: test a bitmap of all-ones 2x2 pixel footprints first")
+    ap.add_argument("--field-masks", choices=["on", "off"], default="on",
+                    help="field: skip the (corner, view) pairs whose factor the carve proved to be 1")
     ap.add_argument("--mc-sizes", default="100,200,300,400,500,600", help="--mode mc: volume sizes")
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--duration", type=float, default=10.0)

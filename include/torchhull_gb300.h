@@ -309,12 +309,17 @@ typedef enum th_option
      * others through the shared persistent carve; 0 (default): every request
      * through the shared carve.  Results are identical. */
     TH_OPTION_BATCH_ROUTE = 3,
-    /* 1 (default): the field stage first builds a bitmap of the 2x2 pixel
-     * footprints whose four mask values are exactly 1 and returns the factor
-     * 1 for a sample there without reading the masks (a bilinear sample of
-     * four ones is exactly 1); 0: every sample reads its four pixels.
+    /* 1 (default): where the field has no cell masks (below), it first
+     * builds a bitmap of the 2x2 pixel footprints whose four mask values are
+     * exactly 1 and returns the factor 1 for a sample there without reading
+     * the masks (a bilinear sample of four ones is exactly 1); 0: every
+     * sample reads its four pixels.  Results are identical. */
+    TH_OPTION_FIELD_ONES = 4,
+    /* 1 (default): the carve's skip and out-of-frame views of the last
+     * level's cells (levels 1 to 10) tell the field which (corner, view)
+     * factors are exactly 1, and it skips them; 0: every pair is evaluated.
      * Results are identical. */
-    TH_OPTION_FIELD_ONES = 4
+    TH_OPTION_FIELD_MASKS = 5
 } th_option;
 th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value);
 th_status th_context_stage_times(const th_context* ctx, th_stage_times* out);

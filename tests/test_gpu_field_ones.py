@@ -1,8 +1,11 @@
-"""All-ones footprint shortcut of the field (TH_OPTION_FIELD_ONES): a sample
-whose 2x2 mask footprint is all ones returns 1 without reading the masks.  The
-field values and meshes must be bit-identical with and without it: full and
-partial masks, binary and blurred (non-binary) masks, every mask dtype,
-OpenCV, more than 32 views, NaN projections, the batched form, and the oracle."""
+"""The field's two exact shortcuts: the cell masks from the carve
+(TH_OPTION_FIELD_MASKS: (corner, view) pairs whose factor is exactly 1 are
+skipped) and, where there are none, the all-ones footprint bitmap
+(TH_OPTION_FIELD_ONES: a sample whose 2x2 mask footprint is all ones returns
+1 without reading the masks).  Field values and meshes must be bit-identical
+with and without them: full and partial masks, binary and blurred
+(non-binary) masks, every mask dtype, OpenCV, more than 32 views, widths that
+are no multiple of 32, NaN projections, the batched form, and the oracle."""
 
 from __future__ import annotations
 
@@ -40,17 +43,28 @@ def field_and_mesh(th, cuda, r, masks=None, transforms=None):
             v.cpu().numpy().view(np.uint32), f.cpu().numpy())
 
 
+# (cell masks, all-ones bitmap): plain evaluation, the bitmap alone, the default
+VARIANTS = [(False, False), (False, True), (True, True)]
+
+
+def set_variant(th, masks, ones):
+    th._C.set_field_masks(0, masks)
+    th._C.set_field_ones(0, ones)
+
+
 def on_off(th, cuda, r, **kw):
-    th._C.set_field_ones(0, False)
+    results = []
     try:
-        off = field_and_mesh(th, cuda, r, **kw)
+        for masks, ones in VARIANTS:
+            set_variant(th, masks, ones)
+            results.append(field_and_mesh(th, cuda, r, **kw))
     finally:
-        th._C.set_field_ones(0, True)
-    on = field_and_mesh(th, cuda, r, **kw)
-    for x, y in zip(on, off, strict=True):
-        assert x.shape == y.shape
-        assert np.array_equal(x, y)
-    return on
+        set_variant(th, True, True)
+    for other in results[1:]:
+        for x, y in zip(other, results[0], strict=True):
+            assert x.shape == y.shape
+            assert np.array_equal(x, y)
+    return results[-1]
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
@@ -93,12 +107,14 @@ def test_batched(th, cuda):
     reqs = [scenes.make_request(**CASES[c]) for c in sorted(CASES)]
     tuples = [(r.masks.to(cuda), r.transforms.to(cuda), r.level, r.cube_corner_bfl, r.cube_length, r.masks_partial,
                r.transforms_convention, True) for r in reqs]
-    th._C.set_field_ones(0, False)
+    results = []
     try:
-        off = [(v.cpu().numpy(), f.cpu().numpy()) for v, f in th._C.visual_hull_batch(tuples)]
+        for masks, ones in VARIANTS:
+            set_variant(th, masks, ones)
+            results.append([(v.cpu().numpy(), f.cpu().numpy()) for v, f in th._C.visual_hull_batch(tuples)])
     finally:
-        th._C.set_field_ones(0, True)
-    on = [(v.cpu().numpy(), f.cpu().numpy()) for v, f in th._C.visual_hull_batch(tuples)]
-    for (va, fa), (vb, fb) in zip(on, off, strict=True):
-        assert np.array_equal(fa, fb)
-        assert np.array_equal(va.view(np.uint32), vb.view(np.uint32))
+        set_variant(th, True, True)
+    for other in results[1:]:
+        for (va, fa), (vb, fb) in zip(other, results[0], strict=True):
+            assert np.array_equal(fa, fb)
+            assert np.array_equal(va.view(np.uint32), vb.view(np.uint32))

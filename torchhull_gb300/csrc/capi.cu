@@ -352,6 +352,7 @@ struct th_context
     bool graphs = true;  // TH_OPTION_GRAPHS
     bool batch_route = false; // TH_OPTION_BATCH_ROUTE
     bool field_ones = true;   // TH_OPTION_FIELD_ONES
+    bool field_masks = true;  // TH_OPTION_FIELD_MASKS
     std::map<th::TuneKey, th::CarveVariants> carve_tuned;
     cudaEvent_t tune_ev[2] = { nullptr, nullptr };
 };
@@ -425,7 +426,7 @@ int64_t max_nodes(int level)
 // Sizes the pools of slot s for request a and fills its plan.
 // batch_slot: the request is part of a batch, whose octree lives in the
 // batch's shared node pool, so the slot keeps no octree pools of its own.
-void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_ones, bool batch_slot = false)
+void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_ones, bool field_masks, bool batch_slot = false)
 {
     const int L = a->level;
     const int64_t B = a->batch, H = a->height, W = a->width;
@@ -454,6 +455,11 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_one
     s.tf.ensure(sizeof(float) * std::max<int64_t>(B, 1) * 16);
     s.sat.ensure(sizeof(float) * std::max<int64_t>(B * H * W, 1));
     const int64_t WW = (W + 31) / 32;
+    // the field's cell-mask table of level L-1 (up to 2^27 cells, 512 MB:
+    // level 10) skips most pairs; the all-ones bitmap only pays without it
+    const bool cell_masks = field_masks && L >= 1 && 3 * (L - 1) <= 27 &&
+                            (a->masks_partial != 0 || (B > 0 && H > 0 && W > 0 && H * W <= (int64_t{ 1 } << 23)));
+    field_ones = field_ones && !cell_masks;
     if (field_ones)
         s.ones.ensure(sizeof(uint32_t) * std::max<int64_t>(B * H * WW, 1));
     s.nodes.ensure(sizeof(int64_t) * node_cap);
@@ -516,10 +522,9 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_one
     // exact integer box sums need every SAT sum of two entries below 2^24
     p.skip_ok = B > 0 && H > 0 && W > 0 && H * W <= (int64_t{ 1 } << 23);
     p.field_ones = field_ones && B > 0 && H > 0 && W > 0;
-    // the cell-mask table of level L-1, up to 2^27 cells (512 MB: level 10)
     p.cell_masks = nullptr;
     p.own_cell_masks = !batch_slot;
-    if (field_ones && L >= 1 && 3 * (L - 1) <= 27 && (p.partial || p.skip_ok))
+    if (cell_masks)
     {
         if (s.cell_masks.ensure(sizeof(uint32_t) * (int64_t{ 1 } << (3 * (L - 1)))))
             TH_CUDA(cudaMemsetAsync(s.cell_masks.p, 0, s.cell_masks.bytes, st));
@@ -689,7 +694,7 @@ void run_hull_once(th_context* ctx,
     const int L = a->level;
     for (int attempt = 0; attempt < 8; ++attempt)
     {
-        prepare(s, a, st, ctx->field_ones);
+        prepare(s, a, st, ctx->field_ones, ctx->field_masks);
         for (int i = 0; i < kMaxLevel; ++i)
             s.plan.carve_variant[i] = variants[i];
         const HullPlan& p = s.plan;
@@ -859,7 +864,7 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
         {
             const th_hull_args* a = &args[r];
             HullSlot& s = ctx->batch[r];
-            prepare(s, a, st, ctx->field_ones, true);
+            prepare(s, a, st, ctx->field_ones, ctx->field_masks, true);
             if (attempt == 0)
             {
                 launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), st);
@@ -1339,6 +1344,8 @@ th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value)
             ctx->batch_route = value != 0;
         else if (option == TH_OPTION_FIELD_ONES && (value == 0 || value == 1))
             ctx->field_ones = value != 0;
+        else if (option == TH_OPTION_FIELD_MASKS && (value == 0 || value == 1))
+            ctx->field_masks = value != 0;
         else
             throw ArgError{ TH_ERR_INVALID_ARGUMENT, "unknown option or value" };
     });

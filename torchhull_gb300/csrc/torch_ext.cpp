@@ -556,6 +556,13 @@ void set_field_ones(int device, bool enable)
     check(th_context_set_option(dc.ctx, TH_OPTION_FIELD_ONES, enable ? 1 : 0), dc.ctx);
 }
 
+void set_field_masks(int device, bool enable)
+{
+    DeviceContext& dc = context_for(device);
+    std::lock_guard<std::mutex> g(dc.lock);
+    check(th_context_set_option(dc.ctx, TH_OPTION_FIELD_MASKS, enable ? 1 : 0), dc.ctx);
+}
+
 // A context of its own (own pools), for callers that run several requests at
 // once on different streams, e.g. a serving loop with one context per slot.
 // The call runs on the current stream of the masks' device, with the GIL
@@ -663,6 +670,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
           "Batched form: run requests that fill the GPU alone through the per-request pipeline (default off).");
     m.def("set_field_ones", &set_field_ones, "device"_a, "enable"_a,
           "Field: skip the mask reads of samples whose 2x2 footprint is all ones (default on).");
+    m.def("set_field_masks", &set_field_masks, "device"_a, "enable"_a,
+          "Field: skip the (corner, view) pairs whose factor the carve proved to be 1 (default on).");
     m.def("set_graphs", &set_graphs, "device"_a, "enable"_a,
           "Replay each request shape's pipeline as a captured CUDA graph (default on).");
     pybind11::class_<HullContext>(m, "HullContext", "Context with its own device pools (one request at a time).")
