@@ -73,8 +73,11 @@ __device__ __forceinline__ void mc_vertex(const McPlan& p, int64_t x, int64_t y,
 #pragma unroll
     for (int a = 0; a < 3; ++a)
     {
-        const float f1 = static_cast<float>(c1[a]);
-        const float f2 = static_cast<float>(c1[a] + (a == axis ? 1 : 0));
+        // exact float conversions by adds below 2^23 (the 64-bit integer
+        // conversions run on GB300's FP64 pipe)
+        const int64_t i1 = c1[a], i2 = c1[a] + (a == axis ? 1 : 0);
+        const float f1 = i1 < 8388608 ? small_i2f(static_cast<int32_t>(i1)) : static_cast<float>(i1);
+        const float f2 = i2 < 8388608 ? small_i2f(static_cast<int32_t>(i2)) : static_cast<float>(i2);
         q[a] = snap == 1 ? f1 : (snap == 2 ? f2 : lerp(f1, f2, t));
         out[a] = p.local ? __fsub_rn(__fmul_rn(q[a], p.scale[a]), 1.f) : q[a];
     }

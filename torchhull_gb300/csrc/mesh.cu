@@ -726,25 +726,31 @@ __device__ __forceinline__ void edge_vertex(const HullPlan& p,
         snap = 2;
     else if (fabsf(__fsub_rn(v1, v2)) < eps)
         snap = 1;
+    // grid coordinates are below 2^13: exact float conversions by adds (the
+    // 64-bit integer conversions run on GB300's FP64 pipe)
+    const float fx1 = small_i2f(static_cast<int32_t>(x1)), fy1 = small_i2f(static_cast<int32_t>(y1)),
+                fz1 = small_i2f(static_cast<int32_t>(z1));
+    const float fx2 = small_i2f(static_cast<int32_t>(x2)), fy2 = small_i2f(static_cast<int32_t>(y2)),
+                fz2 = small_i2f(static_cast<int32_t>(z2));
     float q[3];
     if (snap == 1)
     {
-        q[0] = static_cast<float>(x1);
-        q[1] = static_cast<float>(y1);
-        q[2] = static_cast<float>(z1);
+        q[0] = fx1;
+        q[1] = fy1;
+        q[2] = fz1;
     }
     else if (snap == 2)
     {
-        q[0] = static_cast<float>(x2);
-        q[1] = static_cast<float>(y2);
-        q[2] = static_cast<float>(z2);
+        q[0] = fx2;
+        q[1] = fy2;
+        q[2] = fz2;
     }
     else
     {
         const float t = __fdiv_rn(__fsub_rn(iso, v1), __fsub_rn(v2, v1));
-        q[0] = lerp(static_cast<float>(x1), static_cast<float>(x2), t);
-        q[1] = lerp(static_cast<float>(y1), static_cast<float>(y2), t);
-        q[2] = lerp(static_cast<float>(z1), static_cast<float>(z2), t);
+        q[0] = lerp(fx1, fx2, t);
+        q[1] = lerp(fy1, fy2, t);
+        q[2] = lerp(fz1, fz2, t);
     }
 #pragma unroll
     for (int a = 0; a < 3; ++a)
