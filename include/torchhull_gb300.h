@@ -267,6 +267,11 @@ th_status th_store_curve_network(th_context* ctx,
  */
 th_status th_visual_hull_batch(th_context* ctx, const th_hull_args* args, int32_t n, void* stream, th_hull_info* infos);
 th_status th_visual_hull_batch_export(th_context* ctx, int32_t index, float* verts, int64_t* faces, void* stream);
+/* The meshes of requests 0..n-1 of the last batch at once (verts[i], faces[i]
+ * sized from infos[i]); the exports run side by side and are joined into
+ * stream before the call's work on it completes. */
+th_status th_visual_hull_batch_export_all(th_context* ctx, int32_t n, float* const* verts, int64_t* const* faces,
+                                          void* stream);
 
 /* Stage timing (no reference counterpart).  With profiling on, th_visual_hull
  * records CUDA events between its stages on the request's stream; the times

@@ -865,13 +865,6 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
             const th_hull_args* a = &args[r];
             HullSlot& s = ctx->batch[r];
             prepare(s, a, st, ctx->field_ones, ctx->field_masks, true);
-            if (attempt == 0)
-            {
-                launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), st);
-                TH_CUDA(cudaMemsetAsync(s.flags.p, 0, sizeof(unsigned int), st));
-                launch_integral_image(a->masks, a->masks_dtype, a->batch, a->height, a->width, s.sat.as<float>(), st,
-                                      s.flags.as<unsigned int>());
-            }
             TH_CUDA(cudaMemsetAsync(s.plan.ctr, 0, sizeof(DevCounters), st));
             const HullPlan& p = s.plan;
             BatchReq& q = bs.host_reqs[r];
@@ -897,6 +890,29 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
             q.R = p.R;
             q.WR = p.WR;
             q.cell_masks = p.cell_masks;
+        }
+        if (attempt == 0)
+        {
+            // the requests' integral images side by side on the streams (each
+            // walks its columns and rows sequentially and leaves the GPU idle)
+            TH_CUDA(cudaEventRecord(bs.fork, st));
+            for (int i = 0; i < nstreams; ++i)
+                TH_CUDA(cudaStreamWaitEvent(bs.streams[i], bs.fork, 0));
+            for (int32_t r = 0; r < n; ++r)
+            {
+                const th_hull_args* a = &args[r];
+                HullSlot& s = ctx->batch[r];
+                cudaStream_t sr = bs.streams[r % nstreams];
+                launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), sr);
+                TH_CUDA(cudaMemsetAsync(s.flags.p, 0, sizeof(unsigned int), sr));
+                launch_integral_image(a->masks, a->masks_dtype, a->batch, a->height, a->width, s.sat.as<float>(), sr,
+                                      s.flags.as<unsigned int>());
+            }
+            for (int i = 0; i < nstreams; ++i)
+            {
+                TH_CUDA(cudaEventRecord(bs.joins[i], bs.streams[i]));
+                TH_CUDA(cudaStreamWaitEvent(st, bs.joins[i], 0));
+            }
         }
         TH_CUDA(cudaMemcpyAsync(bs.reqs.p, bs.host_reqs, sizeof(BatchReq) * n, cudaMemcpyHostToDevice, st));
         BatchPlan bp{};
@@ -1619,6 +1635,50 @@ th_status th_visual_hull_batch_export(th_context* ctx, int32_t index, float* ver
             launch_export(s.plan, verts, faces, st);
         }
         TH_CUDA(cudaEventRecord(s.done, st));
+    });
+}
+
+th_status th_visual_hull_batch_export_all(th_context* ctx, int32_t n, float* const* verts, int64_t* const* faces,
+                                          void* stream)
+{
+    return guarded(ctx, [&] {
+        if (n < 0 || n > static_cast<int32_t>(ctx->batch.size()))
+            throw ArgError{ TH_ERR_STATE, "no batched result for that many requests" };
+        if (n > 0 && (!verts || !faces))
+            throw ArgError{ TH_ERR_INVALID_ARGUMENT, "verts or faces array is NULL" };
+        for (int32_t i = 0; i < n; ++i)
+        {
+            if (!ctx->batch[i].has_result)
+                throw ArgError{ TH_ERR_STATE, "no batched result at this index" };
+            if (ctx->batch[i].info.num_faces > 0 && (!verts[i] || !faces[i]))
+                throw ArgError{ TH_ERR_INVALID_ARGUMENT, "verts or faces pointer is NULL" };
+        }
+        auto st = static_cast<cudaStream_t>(stream);
+        BatchState& bs = ctx->bstate;
+        const int ns = std::min<int>(n, static_cast<int>(bs.streams.size()));
+        if (ns > 1)
+        {
+            // the exports side by side on the batch's streams, joined back into st
+            TH_CUDA(cudaEventRecord(bs.fork, st));
+            for (int i = 0; i < ns; ++i)
+                TH_CUDA(cudaStreamWaitEvent(bs.streams[i], bs.fork, 0));
+        }
+        for (int32_t i = 0; i < n; ++i)
+        {
+            HullSlot& s = ctx->batch[i];
+            if (s.info.num_faces > 0)
+                launch_export(s.plan, verts[i], faces[i], ns > 1 ? bs.streams[i % ns] : st);
+        }
+        if (ns > 1)
+        {
+            for (int i = 0; i < ns; ++i)
+            {
+                TH_CUDA(cudaEventRecord(bs.joins[i], bs.streams[i]));
+                TH_CUDA(cudaStreamWaitEvent(st, bs.joins[i], 0));
+            }
+        }
+        for (int32_t i = 0; i < n; ++i)
+            TH_CUDA(cudaEventRecord(ctx->batch[i].done, st));
     });
 }
 

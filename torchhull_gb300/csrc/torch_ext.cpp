@@ -515,15 +515,17 @@ std::vector<std::tuple<at::Tensor, at::Tensor>> visual_hull_batch(const pybind11
     }
     check(st, dc.ctx);
     const auto opts = at::TensorOptions().device(keep[0].device());
+    std::vector<float*> vp(n);
+    std::vector<int64_t*> fp(n);
     for (int64_t i = 0; i < n; ++i)
     {
         at::Tensor v = at::empty({ infos[i].num_verts, 3 }, opts.dtype(at::kFloat));
         at::Tensor f = at::empty({ infos[i].num_faces, 3 }, opts.dtype(at::kLong));
-        check(th_visual_hull_batch_export(dc.ctx, static_cast<int32_t>(i), v.data_ptr<float>(), f.data_ptr<int64_t>(),
-                                          stream),
-              dc.ctx);
+        vp[i] = v.data_ptr<float>();
+        fp[i] = f.data_ptr<int64_t>();
         out.emplace_back(v, f);
     }
+    check(th_visual_hull_batch_export_all(dc.ctx, static_cast<int32_t>(n), vp.data(), fp.data(), stream), dc.ctx);
     return out;
 }
 
