@@ -221,6 +221,11 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchP
             }
             __syncwarp();
         }
+        // The children of the last level are the leaves of the requests that
+        // end there: batch_mark_kernel marks their corners from child_masks,
+        // so they are not written out.
+        if (li + 1 == bp.max_level)
+            break;
         grid.sync();
         // Phase B: the refined children of level li, in parent order (like
         // the plain path's compaction), so that neighbouring cells stay
@@ -298,10 +303,11 @@ __global__ void __launch_bounds__(256) batch_mark_kernel(BatchPlan bp)
     }
     starts[bp.max_level + 1] = s;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    // only the lists of the levels some request ends at
+    // only the lists of the levels some request ends at; the carve writes no
+    // list for the last level (max_level > 0)
     for (int li = 0; li <= bp.max_level; ++li)
     {
-        if (!((bp.leaf_levels >> li) & 1u))
+        if (!((bp.leaf_levels >> li) & 1u) || (li == bp.max_level && li > 0))
             continue;
         const int64_t m = (int64_t{ 1 } << li) - 1;
         for (int64_t t = starts[li] + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < starts[li + 1];
@@ -313,6 +319,32 @@ __global__ void __launch_bounds__(256) batch_mark_kernel(BatchPlan bp)
                 continue;
             const int64_t cell = node & kCellMask;
             mark_cell_corners(q.bitmap, q.rowbits, q.R, q.WR, cell & m, (cell >> li) & m, cell >> (2 * li));
+        }
+    }
+    // the leaves of the requests that end at max_level: the refined children
+    // of the last carved level's cells, from their child masks
+    if (bp.max_level > 0)
+    {
+        const int li = bp.max_level - 1;
+        const int64_t m = (int64_t{ 1 } << li) - 1;
+        for (int64_t t = starts[li] + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < starts[li + 1];
+             t += stride)
+        {
+            uint32_t mask = bp.child_masks[t - starts[li]];
+            if (!mask)
+                continue;
+            const int64_t node = bp.nodes[t];
+            const BatchReq& q = bp.reqs[static_cast<int>(node >> kTagShift)];
+            if (q.level != bp.max_level)
+                continue;
+            const int64_t cell = node & kCellMask;
+            const int64_t x = 2 * (cell & m), y = 2 * ((cell >> li) & m), z = 2 * (cell >> (2 * li));
+            while (mask)
+            {
+                const int k = __ffs(mask) - 1;
+                mask &= mask - 1;
+                mark_cell_corners(q.bitmap, q.rowbits, q.R, q.WR, x + (k & 1), y + (k >> 1 & 1), z + (k >> 2 & 1));
+            }
         }
     }
 }
