@@ -59,17 +59,18 @@ __device__ __forceinline__ ItemResult batch_item(const BatchReq& q,
                                                  const float wz[3],
                                                  bool want_skip,
                                                  bool skip_inside,
-                                                 bool want_out)
+                                                 bool want_out,
+                                                 int grow)
 {
     const ViewSource src = make_view_source(q.tf, q.sat, q.H, q.W);
     if constexpr (VARIANT >= 0)
         return classify_item<(VARIANT >> 1) != 0, (VARIANT & 1) != 0>(src, b, wx, wy, wz, want_skip, skip_inside,
-                                                                      want_out);
+                                                                      want_out, grow);
     if (q.partial)
-        return q.opengl ? classify_item<true, true>(src, b, wx, wy, wz, want_skip, skip_inside, want_out)
-                        : classify_item<true, false>(src, b, wx, wy, wz, want_skip, skip_inside, want_out);
-    return q.opengl ? classify_item<false, true>(src, b, wx, wy, wz, want_skip, skip_inside, want_out)
-                    : classify_item<false, false>(src, b, wx, wy, wz, want_skip, skip_inside, want_out);
+        return q.opengl ? classify_item<true, true>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow)
+                        : classify_item<true, false>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow);
+    return q.opengl ? classify_item<false, true>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow)
+                    : classify_item<false, false>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow);
 }
 
 // Entries of level li that were written (a pool overflow drops the rest).
@@ -161,7 +162,8 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchP
                     produce = qq.skip_ok && (*qq.nonbinary == 0) && (li + 1 < qq.level);
                     const bool skip_inside = qq.partial != 0;
                     const bool want_out = qq.partial && (li + 1 < qq.level) && b < 32;
-                    res = batch_item<VARIANT>(qq, b, wx, wy, wz, produce && b < 32, skip_inside, want_out);
+                    const int grow = li + 2 == qq.level ? 1 : 2;
+                    res = batch_item<VARIANT>(qq, b, wx, wy, wz, produce && b < 32, skip_inside, want_out, grow);
                     if (res.out == 0xffu)
                         atomicOr(&ws.cout_all[s], 1u << b);
                     else

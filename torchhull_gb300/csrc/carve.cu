@@ -105,6 +105,7 @@ struct LevelInfo
     bool produce;     // compute the children's skip masks (the next level consumes them)
     bool skip_inside; // partial mode: the skip rule also wants the corners in frame
     bool produce_out; // compute the children's out-of-frame masks (partial; the next level consumes them)
+    int skip_grow;    // margin of the children's skip rule: 1 when their children are leaves, else 2
 };
 
 __device__ __forceinline__ LevelInfo level_info(const HullPlan& p, int li, bool partial)
@@ -123,6 +124,7 @@ __device__ __forceinline__ LevelInfo level_info(const HullPlan& p, int li, bool 
     L.produce = L.skips && (li + 1 < p.level) && p.carve_variant[li + 1] == 1;
     L.skip_inside = partial;
     L.produce_out = partial && (li + 1 < p.level) && p.carve_variant[li + 1] == 1;
+    L.skip_grow = li + 2 == p.level ? 1 : 2;
     return L;
 }
 
@@ -162,8 +164,8 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_views_kernel
             const ViewSource src = make_view_source(p.tf, p.sat, p.H, p.W);
             for (int64_t b = sub; b < p.B; b += LANES)
             {
-                const ItemResult r =
-                        classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, produce, L.skip_inside, produce_out);
+                const ItemResult r = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, produce, L.skip_inside,
+                                                                    produce_out, L.skip_grow);
                 empty |= r.empty;
                 refine |= r.refine;
                 inside |= r.inside;
@@ -283,7 +285,7 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel
                 lattice_world(p.rq->corner, p.rq->length, is, li, L.inv_rc, wx, wy, wz);
                 const ViewSource src = make_view_source(p.tf, p.sat, p.H, p.W);
                 res = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, L.produce && b < 32, L.skip_inside,
-                                                     L.produce_out && b < 32);
+                                                     L.produce_out && b < 32, L.skip_grow);
                 if (res.out == 0xffu)
                     atomicOr(&ws.cout_all[s], 1u << b);
                 else

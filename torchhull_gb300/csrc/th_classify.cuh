@@ -63,7 +63,7 @@ struct ViewResult
 // want_skip: evaluate the skip rule (the caller checked corners in front and,
 // if needed, two pixels inside).  1 <= H, W < 2^23; Hf, Wf the same as floats.
 template <bool PARTIAL>
-__device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sat_b, int32_t H, int32_t W, float Hf, float Wf, Box bb, bool want_skip)
+__device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sat_b, int32_t H, int32_t W, float Hf, float Wf, Box bb, bool want_skip, int grow = 2)
 {
     const float margin = 0.5f - 0.1f; // isolevel - epsilon (visual_hull_cuda.cu:259-267)
     bb.minx = fminf(FLT_MAX, bb.minx);
@@ -134,13 +134,14 @@ __device__ __forceinline__ ViewResult classify_view(const float* __restrict__ sa
         res.cls = kObject;
     else if (!PARTIAL || (y1.i - y0.i > 1 && x1.i - x0.i > 1))
         res.cls = kRefine;
-    if (want_skip && res.cls == kObject && framed && x0.i >= 2 && y0.i >= 2 && x1.i <= W - 3 && y1.i <= H - 3 &&
-        x0.i <= x1.i && y0.i <= y1.i)
+    if (want_skip && res.cls == kObject && framed && x0.i >= grow && y0.i >= grow && x1.i <= W - 1 - grow &&
+        y1.i <= H - 1 - grow && x0.i <= x1.i && y0.i <= y1.i)
     {
-        // the box grown by two pixels is inside the image: all ones there?
-        const int32_t gx0 = x0.i - 2, gy0 = y0.i - 2, gx1 = x1.i + 2, gy1 = y1.i + 2;
+        // the box grown by `grow` pixels is inside the image: all ones there?
+        const int32_t gx0 = x0.i - grow, gy0 = y0.i - grow, gx1 = x1.i + grow, gy1 = y1.i + grow;
         const float grown = box_sum(sat_b, W, gx0, gy0, gx1, gy1);
-        res.skip = grown == __fmul_rn(__fadd_rn(__fsub_rn(y1.f, y0.f), 5.f), __fadd_rn(__fsub_rn(x1.f, x0.f), 5.f));
+        const float g2 = grow == 1 ? 3.f : 5.f; // 2 * grow + 1
+        res.skip = grown == __fmul_rn(__fadd_rn(__fsub_rn(y1.f, y0.f), g2), __fadd_rn(__fsub_rn(x1.f, x0.f), g2));
     }
     return res;
 }
@@ -243,7 +244,10 @@ __device__ __forceinline__ ViewSource make_view_source(const float* tf, const fl
 // One (parent, view) item: the parent's lattice projected into view b.
 // want_skip: compute the children's skip bits; skip_inside: the skip rule also
 // needs the child's corners two pixels inside the frame; want_out (partial
-// mode): compute the children's out-of-frame bits (box_out).
+// mode): compute the children's out-of-frame bits (box_out); grow: the skip
+// rule's margin in pixels, 2 for masks inherited by all descendants, 1 for the
+// children whose own children are leaves (one level below them, and the
+// field's bilinear footprints of the leaves' corners, stay within one pixel).
 template <bool PARTIAL, bool OPENGL>
 __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                                                     int64_t b,
@@ -252,7 +256,8 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                                                     const float wz[3],
                                                     bool want_skip,
                                                     bool skip_inside,
-                                                    bool want_out = false)
+                                                    bool want_out = false,
+                                                    int grow = 2)
 {
     const int32_t H = static_cast<int32_t>(p.H), W = static_cast<int32_t>(p.W);
     const float Hf = p.Hf, Wf = p.Wf;
@@ -353,7 +358,7 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                 const bool in2 = (prev_in2 & cur_in2 & cbit) != 0;
                 const Box cb = merge(prev[c], cur[c]);
                 const ViewResult r = classify_view<PARTIAL>(sat_b, H, W, Hf, Wf, cb,
-                                                            want_skip && front && (!skip_inside || in2));
+                                                            want_skip && front && (!skip_inside || in2), grow);
                 if (want_out && front && box_out(cb, Hf, Wf))
                     out.out |= bit;
                 if (r.cls == kEmpty)
