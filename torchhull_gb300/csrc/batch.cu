@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(256) batch_mark_kernel(BatchPlan bp)
         for (int64_t t = starts[li] + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < starts[li + 1];
              t += stride)
         {
-            uint32_t mask = bp.child_masks[t - starts[li]];
+            const uint32_t mask = bp.child_masks[t - starts[li]];
             if (!mask)
                 continue;
             const int64_t node = bp.nodes[t];
@@ -340,13 +340,8 @@ __global__ void __launch_bounds__(256) batch_mark_kernel(BatchPlan bp)
             if (q.level != bp.max_level)
                 continue;
             const int64_t cell = node & kCellMask;
-            const int64_t x = 2 * (cell & m), y = 2 * ((cell >> li) & m), z = 2 * (cell >> (2 * li));
-            while (mask)
-            {
-                const int k = __ffs(mask) - 1;
-                mask &= mask - 1;
-                mark_cell_corners(q.bitmap, q.rowbits, q.R, q.WR, x + (k & 1), y + (k >> 1 & 1), z + (k >> 2 & 1));
-            }
+            mark_children_corners(q.bitmap, q.rowbits, q.R, q.WR, 2 * (cell & m), 2 * ((cell >> li) & m),
+                                  2 * (cell >> (2 * li)), mask);
         }
     }
 }

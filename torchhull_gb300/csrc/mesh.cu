@@ -95,13 +95,8 @@ __global__ void __launch_bounds__(256) mark_corners_kernel(HullPlan p)
         if (!m)
             continue;
         const int64_t idx = parents[t];
-        const int64_t x = 2 * (idx & (r - 1)), y = 2 * ((idx >> li) & (r - 1)), z = 2 * (idx >> (2 * li));
-        while (m)
-        {
-            const int k = __ffs(m) - 1;
-            m &= m - 1;
-            mark_cell_corners(p.bitmap, p.rowbits, p.R, p.WR, x + (k & 1), y + (k >> 1 & 1), z + (k >> 2 & 1));
-        }
+        mark_children_corners(p.bitmap, p.rowbits, p.R, p.WR, 2 * (idx & (r - 1)), 2 * ((idx >> li) & (r - 1)),
+                              2 * (idx >> (2 * li)), m);
     }
 }
 

@@ -165,6 +165,48 @@ __device__ __forceinline__ void mark_cell_corners(uint64_t* bitmap, uint32_t* ro
             atomicOr(rowbits + (row >> 5), rb);
     }
 }
+// Sets the corner bits of the refined children (child mask m) of a cell whose
+// lattice starts at (x, y, z) at resolution 2^L: per lattice row (y + dy,
+// z + dz) one OR of the x bits its children cover, instead of four words per
+// child (neighbouring children share 27 of their 64 corners).
+__device__ __forceinline__ void mark_children_corners(uint64_t* bitmap, uint32_t* rowbits, int64_t R, int64_t WR,
+                                                      int64_t x, int64_t y, int64_t z, uint32_t m)
+{
+#pragma unroll
+    for (int dz = 0; dz < 3; ++dz)
+    {
+#pragma unroll
+        for (int dy = 0; dy < 3; ++dy)
+        {
+            uint32_t xb = 0; // lattice x bits 0..2 of this row
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+            {
+                const int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
+                if (((m >> c) & 1u) && (dy == cy || dy == cy + 1) && (dz == cz || dz == cz + 1))
+                    xb |= 3u << cx;
+            }
+            if (!xb)
+                continue;
+            const int64_t row = (y + dy) + (z + dz) * R;
+            const int64_t w = row * WR + (x >> 6);
+            const int b = static_cast<int>(x & 63);
+            const uint64_t lo = static_cast<uint64_t>(xb) << b;
+            if (lo && (bitmap[w] & lo) != lo)
+                atomicOr(reinterpret_cast<unsigned long long*>(bitmap + w), static_cast<unsigned long long>(lo));
+            if (b > 61)
+            {
+                const uint64_t hi = static_cast<uint64_t>(xb) >> (64 - b);
+                if (hi && (bitmap[w + 1] & hi) != hi)
+                    atomicOr(reinterpret_cast<unsigned long long*>(bitmap + w + 1), static_cast<unsigned long long>(hi));
+            }
+            const uint32_t rb = 1u << (row & 31);
+            if (!(rowbits[row >> 5] & rb))
+                atomicOr(rowbits + (row >> 5), rb);
+        }
+    }
+}
+
 void launch_field(const HullPlan& p, cudaStream_t s);
 void launch_marching_cubes(const HullPlan& p, cudaStream_t s);
 void launch_export(const HullPlan& p, float* verts, int64_t* faces, cudaStream_t s);
