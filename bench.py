@@ -64,6 +64,9 @@ METRIC = "hulls/s, level 9, 32x1024^2 views, partial masks (batched form; plain 
 WORKLOAD = ("partial-view visual hull: 32 views of 1024x1024 float32 masks, level 9, masks_partial=True, "
             "unique_verts=True, OpenGL, 8 ellipsoids + 20 capsules")
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
+# DRAM bytes (read + write) per launch of a stage's dominant kernel, from one ncu capture of the
+# same workload (profiles/classify_items_level8_32x1024_partial.md: 60.1 MB read, 1.2 MB written)
+NCU_TRAFFIC = {"carve_level_8": 61.3e6}
 
 
 def peaks() -> tuple[float, str]:
@@ -437,7 +440,7 @@ def run_gb300(args) -> dict | None:
                         "path": "th_visual_hull_batch per step, copies in, batch, meshes out, not overlapped"},
         "roofline": {"bound": "hbm", "kernel": dom[1], "stage": dom[0], "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "algorithmic_bytes": dom[3], "ms": dom[2], "traffic": None,
+                     "algorithmic_bytes": dom[3], "ms": dom[2], "traffic": NCU_TRAFFIC.get(dom[0]),
                      "every_pair_bytes": dom[4],
                      "note": "bytes of the units the kernels evaluate; every_pair_bytes counts every (cell, view) "
                              "or (corner, view) pair, as the reference evaluates them"},
