@@ -65,8 +65,9 @@ WORKLOAD = ("partial-view visual hull: 32 views of 1024x1024 float32 masks, leve
             "unique_verts=True, OpenGL, 8 ellipsoids + 20 capsules")
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 # DRAM bytes (read + write) per launch of a stage's dominant kernel, from one ncu capture of the
-# same workload (profiles/classify_items_level8_32x1024_partial.md: 60.1 MB read, 1.2 MB written)
-NCU_TRAFFIC = {"carve_level_8": 61.3e6}
+# same workload's first request (profiles/classify_items_level8_32x1024_partial.md: 59.8 MB read,
+# 1.3 MB written for its 3.05 M level-8 items)
+NCU_TRAFFIC = {"carve_level_8": 61.1e6}
 
 
 def peaks() -> tuple[float, str]:
