@@ -355,10 +355,14 @@ struct ChildEmit
             return;
         const DevCounters* c = p.ctr;
         const int64_t mask = (int64_t{ 1 } << li) - 1;
-        const int64_t idx = p.nodes[c->level_off[li] + i];
+        // Read-only loads: this launch writes only the next level's slots
+        // (from level_off[li + 1] on), never this level's nodes or the
+        // parents' child masks, so the loads of one chunk of items need not
+        // wait for the stores of the previous one.
+        const int64_t idx = __ldg(p.nodes + c->level_off[li] + i);
         const int64_t gx = 2 * (idx & mask), gy = 2 * ((idx >> li) & mask), gz = 2 * (idx >> (2 * li));
         const int sh = li + 1; // children ravel at resolution 2^(li+1)
-        const uint32_t m = p.child_masks[i];
+        const uint32_t m = __ldg(p.child_masks + i);
         // the masks of the children of the last level (the leaves) are never read
         const bool has_skip = i < p.parent_cap && li + 1 < p.level;
         int64_t out = c->level_off[li + 1] + static_cast<int64_t>(off);
@@ -370,8 +374,8 @@ struct ChildEmit
                 if (out < p.node_cap)
                 {
                     p.nodes[out] = (gx + (k & 1)) | ((gy + (k >> 1 & 1)) << sh) | ((gz + (k >> 2 & 1)) << (2 * sh));
-                    p.node_skip[out] = has_skip ? p.child_skip[i * 8 + k] : 0u;
-                    p.node_out[out] = has_skip ? p.child_out[i * 8 + k] : 0u;
+                    p.node_skip[out] = has_skip ? __ldg(p.child_skip + i * 8 + k) : 0u;
+                    p.node_out[out] = has_skip ? __ldg(p.child_out + i * 8 + k) : 0u;
                 }
                 ++out;
             }
