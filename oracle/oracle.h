@@ -9,12 +9,12 @@
 // host, step by step and with the same float arithmetic, so that its results
 // can be compared bit for bit with the GPU path.  Every function cites the
 // reference file:line it follows.  Parity pinning: the reference ships no
-// golden vectors and cannot be built here (its CUDA build needs glm, stdgpu
-// and charonload, none of which exist offline), so this oracle is pinned only
-// against the reference's own property tests (empty/full masks, closed
-// 2-manifold meshes, soup sizes, OpenGL vs OpenCV agreement, blur identity
-// and dense/sparse agreement); bit-level parity with the reference's own CUDA
-// build is unpinned.
+// golden vectors, so its own CUDA extension is compiled from its unmodified
+// sources (oracle/ref_build.py, with project-written stand-ins for the glm and
+// stdgpu surface it uses) and this oracle is held, bit for bit, to that
+// build's outputs: live on the GPU (tests/test_gpu_reference.py, up to the
+// 32-view 1024^2 level-9 partial scene) and through fixtures the build wrote
+// (tests/golden/ref_*.npz, checked on the CPU by tests/test_ref_golden_cpu.py).
 #pragma once
 
 #include <stdint.h>

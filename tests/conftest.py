@@ -28,3 +28,17 @@ def th():
     import torchhull_gb300
 
     return torchhull_gb300
+
+
+@pytest.fixture(scope="session")
+def ref(cuda):
+    """torchhull's own CUDA extension, built from its unmodified sources by oracle/ref_build.py.
+
+    Skipped where the sources were not staged into oracle/_ref/src; a staged
+    tree that fails to build is an error, not a skip.
+    """
+    from oracle import ref_build
+
+    if not ref_build.staged():
+        pytest.skip("reference sources not staged (oracle/_ref/src)")
+    return ref_build.build(verbose=False)

@@ -1,4 +1,4 @@
-"""CPU checks of the oracle: the reference's own property tests, known answers and the golden fixtures.
+"""CPU checks of the oracle: the reference's own property tests and known answers.
 
 The reference's tests (tests/test_visual_hull.py, tests/test_gaussian_blur.py)
 pin properties, not values; they are restated here against the oracle on the
@@ -12,7 +12,6 @@ import pytest
 import torch
 
 from oracle import oracle
-from tests.golden import make_golden
 from torchhull_gb300 import scenes
 
 
@@ -166,28 +165,6 @@ def test_hull_argument_errors(small):
         oracle.visual_hull(small.masks, small.transforms, 3, (-1, -1, -1), 2.0, False, "vulkan")
     with pytest.raises(RuntimeError):
         oracle.visual_hull(small.masks.to(torch.bool), small.transforms, 3, (-1, -1, -1), 2.0, False, "opengl")
-
-
-@pytest.mark.parametrize("name", list(make_golden.CASES))
-def test_golden_fixtures(name):
-    d = make_golden.load_hull(name)
-    level, partial, opengl, unique = (int(v) for v in d["params"])
-    res = oracle.visual_hull(d["masks"], d["transforms"], level, tuple(d["corner"]), float(d["length"][0]),
-                             bool(partial), "opengl" if opengl else "opencv", bool(unique))
-    assert np.array_equal([lv.size for lv in res.levels], d["level_sizes"])
-    assert np.array_equal(res.field_indices, d["field_indices"])
-    assert np.array_equal(res.field_values, d["field_values"])
-    assert np.array_equal(res.verts, d["verts"])
-    assert np.array_equal(res.faces, d["faces"])
-
-
-def test_golden_blur():
-    z = np.load(make_golden.HERE / "blur_k3_k9.npz")
-    shape = tuple(z["masks_shape"])
-    masks = np.unpackbits(z["masks_bits"])[: int(np.prod(shape))].reshape(shape).astype(np.float32)
-    for k in (3, 9):
-        out = oracle.gaussian_blur(masks, k, 2.0, True, dtype="float32")
-        assert np.abs(out - z[f"sparse_k{k}"]).max() <= 1e-6
 
 
 def test_thread_count_does_not_change_results(small):

@@ -49,17 +49,39 @@ def _load_extension():
     return module
 
 
-_C = _load_extension()
+_ext = None
 
-visual_hull = _C.visual_hull
-visual_hull_with_candidate_voxels = _C.visual_hull_with_candidate_voxels
-gaussian_blur = _C.gaussian_blur
-integral_image = _C.integral_image
-marching_cubes = _C.marching_cubes
-candidate_voxels_to_wireframes = _C.candidate_voxels_to_wireframes
-store_curve_network = _C.store_curve_network
-# beyond the reference: the blur -> hull request of its second benchmark configuration in one call
-visual_hull_blurred = _C.visual_hull_blurred
+# The names re-exported from the extension (the reference's public API plus
+# the fused blur -> hull request of its second benchmark configuration).
+_EXPORTS = (
+    "visual_hull",
+    "visual_hull_with_candidate_voxels",
+    "gaussian_blur",
+    "integral_image",
+    "marching_cubes",
+    "candidate_voxels_to_wireframes",
+    "store_curve_network",
+    "visual_hull_blurred",
+)
+
+
+def _extension():
+    """The CUDA extension, loaded on first use (ImportError when it is not built)."""
+    global _ext
+    if _ext is None:
+        _ext = _load_extension()
+    return _ext
+
+
+def __getattr__(name: str):
+    # Loading on first use keeps the scene generator (``torchhull_gb300.scenes``)
+    # importable without the CUDA extension; every operation still fails loudly
+    # when the extension is missing.
+    if name == "_C":
+        return _extension()
+    if name in _EXPORTS:
+        return getattr(_extension(), name)
+    raise AttributeError(f"module {__name__!r} has no attribute {name!r}")
 
 
 def sparse_visual_hull_field(
@@ -76,7 +98,7 @@ def sparse_visual_hull_field(
     Indices are (0, z, y, x), values the product of the views' mask samples
     (reference: visual_hull_cuda.cu:522-580, :896-914).
     """
-    idx, values, r = _C.sparse_visual_hull_field_raw(
+    idx, values, r = _extension().sparse_visual_hull_field_raw(
         masks, transforms, level, cube_corner_bfl, cube_length, masks_partial, transforms_convention
     )
     z = idx // (r * r)
