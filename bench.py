@@ -32,15 +32,25 @@ U{256,512,768,1024}, level U{6..9}, partial ~ Bernoulli(0.3)), batched vs plain.
 level 8) as one fused request against blur and hull as two calls.
 --mode mc: torchhull.marching_cubes on the reference benchmark's sphere SDF
 volumes (100^3 .. 600^3, dense and sparse), ms per call.
---mode serve: Poisson arrivals (default 200/s for 10 s) from a pool of
+--mode serve: Poisson arrivals (default 200/s for 20 s) from a pool of
 pregenerated requests of the heterogeneous distribution plus 2 % large ones
 (64 views of 2048^2, level 10) through the continuous-batching server (60 GB
 admission budget), against the same stream served one request at a time.
 
-Reference arm: the reference has no CPU path and its CUDA build cannot be
-built here, so it times the CPU restatement of the reference's algorithm
-(oracle/) with all host threads.  One step is one octant of the cube at the
-same leaf size (level 8 over half the cube length): 8 steps cover one hull.
+Also in the headline line (one GPU): `reference_cuda`, torchhull's own CUDA
+extension built from its unmodified sources (oracle/ref_build.py) timed on the
+same requests, one per call, as the comparison point of the plain drop-in;
+`cfg1` (8 views of 256^2, level 6) and `cfg2` (the blur configuration, fused
+and as two calls, and the reference's two calls); `hetero64` (the 64-request
+mix, batched against plain); `serve` (Poisson arrivals at 200/s for 20 s with
+2 % large requests, host inputs copied in inside the latency, continuous
+batching against one request at a time).
+
+Reference arm (--impl reference): the reference has no CPU path, so it times
+the CPU restatement of the reference's algorithm (oracle/) with all host
+threads.  One step is one octant of the cube at the same leaf size (level 8
+over half the cube length): 8 steps cover one hull.  The GB300 arm's
+`cpu_baseline` times the same 8 octants.
 """
 
 from __future__ import annotations
@@ -66,9 +76,11 @@ WORKLOAD = ("partial-view visual hull: 32 views of 1024x1024 float32 masks, leve
             "unique_verts=True, OpenGL, 8 ellipsoids + 20 capsules")
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 # DRAM bytes (read + write) per launch of a stage's dominant kernel, from one ncu capture of the
-# same workload's first request (profiles/classify_items_level8_32x1024_partial.md: 59.8 MB read,
-# 1.3 MB written for its 3.05 M level-8 items)
+# same workload's first request (not measured by this run): dram__bytes_read.sum +
+# dram__bytes_write.sum of the level-8 classify_items_kernel launch.
 NCU_TRAFFIC = {"carve_level_8": 61.1e6}
+NCU_TRAFFIC_SOURCE = ("ncu --set full capture of classify_items_kernel, level 8, first request of this workload "
+                      "(dram__bytes_read.sum + dram__bytes_write.sum); a separate capture, not this run")
 
 
 def peaks() -> tuple[float, str]:
@@ -411,6 +423,13 @@ def run_gb300(args) -> dict | None:
             batch_in(k + 2)
     torch.cuda.synchronize()
     e2e_batched = Q * e2e_steps * world / max_over_ranks(time.perf_counter() - t0, world, dev)
+    del slots, host_out, out, first
+
+    # the other configurations and the reference's CUDA build, measured after the timed region
+    # (one GPU only: under torchrun every rank times the headline alone)
+    extras = {}
+    if world == 1 and not args.no_extras:
+        extras = headline_extras(args, th, scenes, dev, world, rank, reqs, plain_value)
 
     if rank != 0:
         return finish(None, world)
@@ -476,12 +495,14 @@ def run_gb300(args) -> dict | None:
         "roofline": {"bound": "hbm", "kernel": dom[1], "stage": dom[0], "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes": dom[3], "ms": dom[2], "traffic": NCU_TRAFFIC.get(dom[0]),
+                     "traffic_source": NCU_TRAFFIC_SOURCE if dom[0] in NCU_TRAFFIC else None,
                      "every_pair_bytes": dom[4],
                      "note": "bytes of the units the kernels evaluate; every_pair_bytes counts every (cell, view) "
                              "or (corner, view) pair, as the reference evaluates them"},
         "clocks": clocks,
         "gpu_launches": launches,
     }
+    line.update(extras)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(reqs[0], samples=args.cpu_samples)
     return finish(line, world)
@@ -495,7 +516,8 @@ def finish(line, world):
     return line
 
 
-def run_hetero(args, th, scenes, dev, world, rank):
+def hetero_measure(args, th, scenes, dev, world, rank) -> dict:
+    """64 heterogeneous requests: one batched call per step against the plain drop-in, one call per request."""
     import torch
 
     reqs = scenes.batched_requests(count=args.hetero_count, seed=4 + 1000 * rank, device=dev)
@@ -505,29 +527,38 @@ def run_hetero(args, th, scenes, dev, world, rank):
         for r in reqs:
             th.visual_hull(**r.kwargs())
     torch.cuda.synchronize()
+    steps = max(1, args.hetero_steps)
     sampler = ClockSampler(dev.index or 0)
     sampler.start()
     launches0 = th._C.launch_count()
-    batch_ms = timed_batches(th, tuples, args.steps, dev, world)
+    batch_ms = timed_batches(th, tuples, steps, dev, world)
     launches = th._C.launch_count() - launches0
     clocks = sampler.stop()
-    plain_ms, per_hull, _ = timed_plain(th, reqs, args.steps, dev, world, dev.index or 0, profile=False)
+    plain_ms, per_hull, _ = timed_plain(th, reqs, steps, dev, world, dev.index or 0, profile=False)
     n = len(reqs)
+    value = n * steps * world / (batch_ms / 1000.0)
+    plain_value = n * steps * world / (plain_ms / 1000.0)
+    return {"value": value, "unit": "hulls/s", "steps": steps, "ms_per_step": batch_ms / steps,
+            "requests_per_step": n,
+            "workload": f"{n} requests: views U{{4..48}}, side U{{256,512,768,1024}}, level U{{6..9}}, "
+                        "masks_partial ~ Bernoulli(0.3), float32, inputs resident",
+            "plain": {"value": plain_value, "unit": "hulls/s", "p50_ms": percentile(per_hull, 50),
+                      "p99_ms": percentile(per_hull, 99)},
+            "batched_over_plain": value / plain_value, "clocks": clocks, "gpu_launches": launches}
+
+
+def run_hetero(args, th, scenes, dev, world, rank):
+    m = hetero_measure(args, th, scenes, dev, world, rank)
     if rank != 0:
         return None
-    value = n * args.steps * world / (batch_ms / 1000.0)
-    plain_value = n * args.steps * world / (plain_ms / 1000.0)
     return {
-        "metric": "hulls/s, 64 heterogeneous requests (batched form)", "value": value, "unit": "hulls/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_ms / args.steps,
+        "metric": "hulls/s, 64 heterogeneous requests (batched form)", "value": m["value"], "unit": "hulls/s",
+        "n_gpus": world, "steps": m["steps"], "warmup": args.warmup, "ms_per_step": m["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded ray-ellipsoid/capsule masks",
-        "config": {"workload": "64 requests: views U{4..48}, side U{256,512,768,1024}, level U{6..9}, "
-                               "masks_partial ~ Bernoulli(0.3), float32", "requests_per_step": n},
-        "plain": {"value": plain_value, "unit": "hulls/s", "p50_ms": percentile(per_hull, 50),
-                  "p99_ms": percentile(per_hull, 99)},
-        "batched_over_plain": value / plain_value,
-        "clocks": clocks, "gpu_launches": launches,
+        "config": {"workload": m["workload"], "requests_per_step": m["requests_per_step"]},
+        "plain": m["plain"], "batched_over_plain": m["batched_over_plain"],
+        "clocks": m["clocks"], "gpu_launches": m["gpu_launches"],
     }
 
 
@@ -622,26 +653,43 @@ def run_blur(args, th, scenes, dev, world, rank):
             "two_calls_ms": out["two_calls"], "fused_over_two_calls": out["two_calls"] / out["fused"]}
 
 
-def run_serve(args, th, scenes, dev, world, rank):
+def serve_measure(args, th, scenes, dev, world, rank, policies=("none", "large_first", "exclusive_large")) -> dict:
+    """Poisson arrivals from a pool of pregenerated requests of the heterogeneous distribution plus 2 %
+    large ones (64 x 2048^2, level 10), their masks and transforms in pinned host memory: each request
+    is copied in by the server inside its measured latency (arrival -> result on the device).  The
+    continuous-batching server against the same stream served one request at a time."""
     import numpy as np
     import torch
 
     from torchhull_gb300.serve import HullServer
 
-    pool = scenes.batched_requests(count=args.serve_pool, seed=6 + 1000 * rank, device=dev)
-    large = [scenes.make_request(9000 + 1000 * rank + i, 64, 2048, 10, False, device=dev)
-             for i in range(args.serve_large)]
+    def to_host(r):
+        return scenes.HullRequest(r.masks.cpu().pin_memory(), r.transforms.cpu().pin_memory(), r.level,
+                                  r.cube_corner_bfl, r.cube_length, r.masks_partial, r.transforms_convention,
+                                  r.unique_verts)
+
+    pool_dev = scenes.batched_requests(count=args.serve_pool, seed=6 + 1000 * rank, device=dev)
+    large_dev = [scenes.make_request(9000 + 1000 * rank + i, 64, 2048, 10, False, device=dev)
+                 for i in range(args.serve_large)]
+    for r in pool_dev + large_dev:  # warm the autotuner and the allocator
+        th.visual_hull(**r.kwargs())
+    torch.cuda.synchronize()
+    pool = [to_host(r) for r in pool_dev]
+    large = [to_host(r) for r in large_dev]
+    del pool_dev, large_dev
+    torch.cuda.empty_cache()
     rng = np.random.default_rng(7 + rank)
     n = int(args.rate * args.duration)
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=n))
     picks = [large[i % len(large)] if (large and rng.random() < 0.02) else pool[int(rng.integers(len(pool)))]
              for i in range(n)]
-    for r in pool + large:  # warm the pools and the autotuner
-        th.visual_hull(**r.kwargs())
-    torch.cuda.synchronize()
 
     def serve(slots, priority="none"):
         with HullServer(device=dev.index or 0, slots=slots, budget_bytes=60e9, priority=priority) as server:
+            for r in pool[:slots] + large[:1]:  # each slot's context allocates its pools once
+                server.submit(r).result()
+            server.latencies_ms.clear()
+            server.queue_ms.clear()
             t0 = time.perf_counter()
             futures = []
             for t, r in zip(arrivals, picks, strict=True):
@@ -652,29 +700,137 @@ def run_serve(args, th, scenes, dev, world, rank):
             for f in futures:
                 f.result()
             wall = time.perf_counter() - t0
-            return n / wall, server.stats()
+            st = server.stats()
+            return {"value": n / wall, "unit": "hulls/s", "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                    "mean_queue_ms": st["mean_queue_ms"], "wall_s": wall}
 
-    rate_cb, stats_cb = serve(args.serve_slots)
-    rate_hp, stats_hp = serve(args.serve_slots, "large_first")
-    rate_ex, stats_ex = serve(args.serve_slots, "exclusive_large")
-    rate_one, stats_one = serve(1)
+    out = {p: serve(args.serve_slots, p) for p in policies}
+    out["one_at_a_time"] = serve(1)
+    head = out[policies[0]]
+    return {"workload": f"Poisson arrivals {args.rate}/s for {args.duration} s ({n} requests); pool of "
+                        f"{args.serve_pool} requests of the heterogeneous distribution + 2% large (64x2048^2, "
+                        "level 10); inputs in pinned host memory, copied in by the server inside the latency",
+            "slots": args.serve_slots, "budget_bytes": 60e9, "requests": n,
+            "value": head["value"], "unit": "hulls/s", "p50_ms": head["p50_ms"], "p99_ms": head["p99_ms"],
+            "policies": out, "served_over_one_at_a_time": head["value"] / out["one_at_a_time"]["value"],
+            "p50_one_at_a_time_over_served": out["one_at_a_time"]["p50_ms"] / head["p50_ms"]}
+
+
+def run_serve(args, th, scenes, dev, world, rank):
+    m = serve_measure(args, th, scenes, dev, world, rank)
     if rank != 0:
         return None
     return {
-        "metric": "hulls/s and p50/p99 ms under Poisson arrivals (continuous batching)", "value": rate_cb,
-        "unit": "hulls/s", "n_gpus": world, "steps": n, "warmup": 1, "ms_per_step": 1000.0 / rate_cb,
+        "metric": "hulls/s and p50/p99 ms under Poisson arrivals (continuous batching)", "value": m["value"],
+        "unit": "hulls/s", "n_gpus": world, "steps": m["requests"], "warmup": 1, "ms_per_step": 1000.0 / m["value"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: pregenerated pool of seeded requests replayed by the arrival stream",
-        "config": {"workload": f"Poisson arrivals {args.rate}/s for {args.duration} s; pool of {args.serve_pool} "
-                               "requests of the heterogeneous distribution + 2% large (64x2048^2, level 10)",
-                   "slots": args.serve_slots, "budget_bytes": 60e9},
-        "p50_ms": stats_cb["p50_ms"], "p99_ms": stats_cb["p99_ms"],
-        "priority": "none (all requests overlap alike)",
-        "large_first": {"value": rate_hp, "p50_ms": stats_hp["p50_ms"], "p99_ms": stats_hp["p99_ms"]},
-        "exclusive_large": {"value": rate_ex, "p50_ms": stats_ex["p50_ms"], "p99_ms": stats_ex["p99_ms"]},
-        "one_at_a_time": {"value": rate_one, "p50_ms": stats_one["p50_ms"], "p99_ms": stats_one["p99_ms"]},
-        "served_over_one_at_a_time": rate_cb / rate_one,
+        "config": {"workload": m["workload"], "slots": m["slots"], "budget_bytes": m["budget_bytes"]},
+        "p50_ms": m["p50_ms"], "p99_ms": m["p99_ms"], "policies": m["policies"],
+        "served_over_one_at_a_time": m["served_over_one_at_a_time"],
     }
+
+
+def time_calls(fn, n: int, warmup: int) -> tuple[float, list[float]]:
+    """(calls/s, sorted per-call ms) of fn on the current stream, CUDA events around each call."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    per: list[float] = []
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(n):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        per.append(e0.elapsed_time(e1))
+    stop.record()
+    torch.cuda.synchronize()
+    return n / (start.elapsed_time(stop) / 1000.0), sorted(per)
+
+
+def reference_cuda_module():
+    """torchhull's own CUDA extension (its unmodified sources compiled by oracle/ref_build.py), or None."""
+    from oracle import ref_build
+
+    if not ref_build.staged():
+        return None
+    return ref_build.build()
+
+
+def reference_cuda_leg(ref, reqs, rounds: int, warmup: int) -> dict:
+    """The reference's own CUDA build on the same requests, one per call on the current stream: the
+    comparison point for the plain drop-in (its results equal the plain path's bit for bit)."""
+    state = {"q": 0}
+
+    def one():
+        r = reqs[state["q"] % len(reqs)]
+        state["q"] += 1
+        ref.visual_hull(*as_tuple(r))
+
+    value, per = time_calls(one, rounds * len(reqs), warmup * len(reqs))
+    return {"value": value, "unit": "hulls/s", "p50_ms": percentile(per, 50), "p99_ms": percentile(per, 99),
+            "hulls": rounds * len(reqs),
+            "path": "torchhull's own CUDA extension built from its unmodified sources (glm/stdgpu stand-ins), "
+                    "visual_hull one request per call"}
+
+
+def headline_extras(args, th, scenes, dev, world, rank, reqs, plain_value) -> dict:
+    """The other configurations, measured in the same run (one GPU): the reference CUDA build on the
+    headline requests, the small and blur configurations, the 64-request mix and the served stream."""
+    import torch
+
+    out: dict = {}
+    ref = reference_cuda_module() if not args.no_reference_cuda else None
+    if ref is not None:
+        leg = reference_cuda_leg(ref, reqs, max(1, min(args.steps, args.ref_rounds)), 1)
+        leg["plain_over_reference_cuda"] = plain_value / leg["value"]
+        out["reference_cuda"] = leg
+    else:
+        out["reference_cuda"] = {"unavailable": "reference sources not staged (oracle/_ref/src)"}
+
+    # 8 OpenGL views of 256^2, level 6, full masks
+    r1 = scenes.small_request(dev)
+    v1, p1 = time_calls(lambda: th.visual_hull(**r1.kwargs()), 50, 5)
+    cfg1 = {"workload": "3 ellipsoids, 8 OpenGL views of 256x256 float32, level 6, full masks",
+            "plain": {"value": v1, "unit": "hulls/s", "p50_ms": percentile(p1, 50), "p99_ms": percentile(p1, 99)}}
+    if ref is not None:
+        rv, rp = time_calls(lambda: ref.visual_hull(*as_tuple(r1)), 20, 3)
+        cfg1["reference_cuda"] = {"value": rv, "unit": "hulls/s", "p50_ms": percentile(rp, 50)}
+        cfg1["plain_over_reference_cuda"] = v1 / rv
+    out["cfg1"] = cfg1
+
+    # blur k=9 sigma=2 then level 8, 24 OpenCV views of 512^2
+    r2 = scenes.blur_request(device=dev)
+    hull_args = (r2.transforms, r2.level, r2.cube_corner_bfl, r2.cube_length, r2.masks_partial,
+                 r2.transforms_convention)
+    fv, fp = time_calls(lambda: th.visual_hull_blurred(r2.masks, *hull_args, 9, 2.0), 30, 5)
+    tv, tp = time_calls(lambda: th.visual_hull(th.gaussian_blur(r2.masks, 9, 2.0), *hull_args), 30, 5)
+    cfg2 = {"workload": "5 ellipsoids, 24 OpenCV views of 512x512 float32, gaussian_blur(k=9, sigma=2, sparse), "
+                        "visual_hull level 8, full masks",
+            "fused": {"value": fv, "unit": "hulls/s", "p50_ms": percentile(fp, 50)},
+            "two_calls": {"value": tv, "unit": "hulls/s", "p50_ms": percentile(tp, 50)}}
+    if ref is not None:
+        rv, rp = time_calls(lambda: ref.visual_hull(ref.gaussian_blur(r2.masks, 9, 2.0, True), *hull_args), 10, 2)
+        cfg2["reference_cuda_two_calls"] = {"value": rv, "unit": "hulls/s", "p50_ms": percentile(rp, 50)}
+        cfg2["fused_over_reference_cuda"] = fv / rv
+    out["cfg2"] = cfg2
+    del r1, r2
+    torch.cuda.empty_cache()
+
+    if not args.no_hetero:
+        out["hetero64"] = hetero_measure(args, th, scenes, dev, world, rank)
+        torch.cuda.empty_cache()
+    if not args.no_serve:
+        out["serve"] = serve_measure(args, th, scenes, dev, world, rank, policies=("none",))
+        torch.cuda.empty_cache()
+    return out
 
 
 def octant_args(o: int):
@@ -682,7 +838,7 @@ def octant_args(o: int):
     return corner, 1.0, LEVEL - 1
 
 
-def cpu_baseline(req, samples: int = 2) -> dict:
+def cpu_baseline(req, samples: int = 8) -> dict:
     from oracle import oracle
 
     masks = req.masks.cpu().numpy()
@@ -690,12 +846,12 @@ def cpu_baseline(req, samples: int = 2) -> dict:
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     for o in range(samples):
-        corner, length, level = octant_args(o)
+        corner, length, level = octant_args(o % 8)
         oracle.visual_hull(masks, tf, level, corner, length, True, "opengl", True, nthreads=threads)
     dt = time.perf_counter() - t0
     return {"value": (samples / 8.0) / dt, "unit": "hulls/s", "cores": threads, "kind": "port",
-            "sample": f"{samples} of the 8 octants of one request (same leaf size: level 8 over half the cube); "
-                      f"{dt:.1f} s"}
+            "sample": f"{samples} octants of one request in turn (each level 8 over half the cube: the same "
+                      f"leaf size; 8 octants = one hull); {dt:.1f} s"}
 
 
 def run_reference(args) -> dict | None:
@@ -737,8 +893,8 @@ def run_reference(args) -> dict | None:
         "dtype": "f32",
         "data": "synthetic: seeded ray-ellipsoid/capsule masks",
         "config": {"workload": WORKLOAD,
-                   "path": "CPU restatement of the reference algorithm (the reference has no CPU path and its "
-                           "CUDA build needs glm/stdgpu/charonload, absent offline)"},
+                   "path": "CPU restatement of the reference algorithm (the reference has no CPU path; its own "
+                           "CUDA build is timed as reference_cuda in the GB300 arm's line)"},
         "cpu_baseline": {"value": value, "unit": "hulls/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "hulls/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -752,11 +908,18 @@ def main() -> None:
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--mode", choices=["headline", "hetero", "serve", "mc", "blur"], default="headline")
     ap.add_argument("--requests", type=int, default=4)
-    ap.add_argument("--cpu-samples", type=int, default=2)
+    ap.add_argument("--cpu-samples", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--carve-kernel", choices=["auto", "views", "items"], default="auto",
                     help="carve kernel: autotuned (default) or forced")
     ap.add_argument("--hetero-count", type=int, default=64)
+    ap.add_argument("--hetero-steps", type=int, default=3)
+    ap.add_argument("--ref-rounds", type=int, default=5,
+                    help="headline: rounds of the Q requests timed through the reference's CUDA build")
+    ap.add_argument("--no-extras", action="store_true", help="headline: skip the other configurations")
+    ap.add_argument("--no-reference-cuda", action="store_true")
+    ap.add_argument("--no-hetero", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--batch-route", choices=["on", "off"], default="off",
                     help="batched form: requests that fill the GPU alone through the per-request pipeline")
     ap.add_argument("--field-ones", choices=["on", "off"], default="on",
@@ -765,7 +928,7 @@ def main() -> None:
                     help="field: skip the (corner, view) pairs whose factor the carve proved to be 1")
     ap.add_argument("--mc-sizes", default="100,200,300,400,500,600", help="--mode mc: volume sizes")
     ap.add_argument("--rate", type=float, default=200.0)
-    ap.add_argument("--duration", type=float, default=10.0)
+    ap.add_argument("--duration", type=float, default=20.0)
     ap.add_argument("--serve-pool", type=int, default=24)
     ap.add_argument("--serve-large", type=int, default=1)
     ap.add_argument("--serve-slots", type=int, default=8)

@@ -75,3 +75,40 @@ def test_gpu_filling_requests_routed_or_shared(th, cuda, route):
                 assert torch.equal(v.cpu(), ev) and torch.equal(f.cpu(), ef)
     finally:
         th._C.set_batch_route(0, False)
+
+
+def test_batch_and_plain_calls_from_two_threads(th, cuda):
+    """A batch on one thread and plain calls on another share the device's context without deadlocking."""
+    import threading
+
+    reqs = [scenes.make_request(550 + i, 16, 256, 7, i % 2 == 0, device=cuda) for i in range(4)]
+    expected = [plain(th, r) for r in reqs]
+    errors: list[BaseException] = []
+    results: dict[str, list] = {"batch": [], "plain": []}
+
+    def batches():
+        try:
+            for _ in range(4):
+                out = th._C.visual_hull_batch([as_tuple(r) for r in reqs])
+                torch.cuda.synchronize()
+                results["batch"].append([(v.cpu(), f.cpu()) for v, f in out])
+        except BaseException as exc:  # reported below
+            errors.append(exc)
+
+    def plains():
+        try:
+            for _ in range(4):
+                results["plain"].append([plain(th, r) for r in reqs])
+        except BaseException as exc:
+            errors.append(exc)
+
+    threads = [threading.Thread(target=batches, daemon=True), threading.Thread(target=plains, daemon=True)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=120)
+    assert not any(t.is_alive() for t in threads), "threads did not finish"
+    assert not errors, errors
+    for run in results["batch"] + results["plain"]:
+        for (v, f), (ev, ef) in zip(run, expected, strict=True):
+            assert torch.equal(v, ev) and torch.equal(f, ef)

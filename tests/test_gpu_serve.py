@@ -69,3 +69,39 @@ def test_unknown_priority_policy_is_refused(cuda):
 
     with pytest.raises(ValueError):
         HullServer(device=cuda.index or 0, slots=1, priority="fastest")
+
+
+def test_submit_without_synchronizing(th, cuda, requests):
+    """Inputs still being written on the submitting thread's stream are waited for, not read early."""
+    from torchhull_gb300.serve import HullServer
+
+    expected = [alone(th, r) for r in requests[:4]]
+    side = torch.cuda.Stream(cuda)
+    with torch.cuda.stream(side), HullServer(device=cuda.index or 0, slots=2) as server:
+        futures = []
+        for r in requests[:4]:
+            busy = torch.randn(4096, 4096, device=cuda)
+            for _ in range(8):  # keep the stream busy before the masks are written
+                busy = busy @ busy.T / 4096.0
+            masks = torch.zeros_like(r.masks)
+            masks.copy_(r.masks)
+            futures.append(server.submit(scenes.HullRequest(masks, r.transforms, r.level, r.cube_corner_bfl,
+                                                            r.cube_length, r.masks_partial,
+                                                            r.transforms_convention)))
+            del masks
+        got = [f.result(timeout=120) for f in futures]
+        got = [(v.cpu(), f.cpu()) for v, f in got]
+    for (v, f), (ev, ef) in zip(got, expected, strict=True):
+        assert torch.equal(v, ev) and torch.equal(f, ef)
+
+
+def test_host_inputs_are_copied_in(th, cuda, requests):
+    from torchhull_gb300.serve import HullServer
+
+    host = [scenes.HullRequest(r.masks.cpu().pin_memory(), r.transforms.cpu(), r.level, r.cube_corner_bfl,
+                               r.cube_length, r.masks_partial, r.transforms_convention) for r in requests]
+    with HullServer(device=cuda.index or 0, slots=3) as server:
+        got = [f.result(timeout=120) for f in [server.submit(r) for r in host]]
+    for r, (v, f) in zip(requests, got, strict=True):
+        ev, ef = alone(th, r)
+        assert v.is_cuda and torch.equal(v.cpu(), ev) and torch.equal(f.cpu(), ef)

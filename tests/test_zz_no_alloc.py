@@ -43,17 +43,34 @@ def noalloc_blur(lib, images: torch.Tensor, k: int, sigma: float, sparse: bool, 
     return rc, out
 
 
+@pytest.mark.parametrize("k", [1, 3, 9])
+@pytest.mark.parametrize("out_dtype", [torch.float16, torch.float32, torch.float64])
 @pytest.mark.parametrize("sparse", [True, False])
-def test_noalloc_matches_blur_twice(cuda, th, lib, sparse):
+def test_noalloc_matches_blur_twice(cuda, th, lib, sparse, out_dtype, k):
     from torchhull_gb300 import scenes
 
     first = scenes.make_request(41, views=3, side=200, level=4, partial=False).masks.to(cuda)
     second = scenes.make_request(42, views=5, side=160, level=4, partial=False, n_ellipsoids=5).masks.to(cuda)
     for masks in (first, second):  # two calls in a row: the shared scratch must not leak between calls
-        rc, got = noalloc_blur(lib, masks, 9, 2.0, sparse, torch.float32)
+        rc, got = noalloc_blur(lib, masks, k, 2.0, sparse, out_dtype)
         torch.cuda.synchronize()
         assert rc == 0
-        want = th.gaussian_blur(masks, 9, 2.0, sparse, torch.float32)
+        want = th.gaussian_blur(masks, k, 2.0, sparse, out_dtype)
+        assert got.dtype == want.dtype == out_dtype
+        assert (got.double() - want.double()).abs().max().item() <= TOL
+
+
+def test_noalloc_just_below_the_scratch_limit(cuda, th, lib):
+    # k=3: B*(H+1)*(W+1) bytes of tile flags + 96 bytes of weights; 4095^2 + 96 = 16,769,121 <= 16 MiB,
+    # so the weights sit in the last few kilobytes of the array
+    n = 4094
+    yy, xx = torch.meshgrid(torch.arange(n, device=cuda), torch.arange(n, device=cuda), indexing="ij")
+    disk = (((yy - n / 2) ** 2 + (xx - n / 2) ** 2) < (0.3 * n) ** 2).to(torch.uint8)[None, :, :, None]
+    for masks in (disk, 1 - disk):
+        rc, got = noalloc_blur(lib, masks.contiguous(), 3, 1.0, True, torch.float32)
+        torch.cuda.synchronize()
+        assert rc == 0
+        want = th.gaussian_blur(masks.contiguous(), 3, 1.0, True, torch.float32)
         assert (got - want).abs().max().item() <= TOL
 
 

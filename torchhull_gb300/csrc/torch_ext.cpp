@@ -58,6 +58,21 @@ DeviceContext& context_for(int device)
     return *dc;
 }
 
+// Takes a context lock on a thread that holds the GIL. Waiting happens with the
+// GIL released: a thread that holds the lock may itself be waiting for the GIL
+// (a batch call re-acquires it on leaving its GIL-free section), so blocking
+// on the lock with the GIL held could deadlock the two threads.
+std::unique_lock<std::mutex> lock_nogil(std::mutex& m)
+{
+    std::unique_lock<std::mutex> lk(m, std::defer_lock);
+    if (!lk.try_lock())
+    {
+        pybind11::gil_scoped_release nogil;
+        lk.lock();
+    }
+    return lk;
+}
+
 void check(th_status st, th_context* ctx)
 {
     if (st == TH_OK)
@@ -179,7 +194,7 @@ HullOutputs run_visual_hull(const at::Tensor& masks_in,
                                transforms_convention, unique_verts);
 
     DeviceContext& dc = context_for(masks.device().index());
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     void* stream = stream_of(masks);
     th_hull_info info{};
     if (blur_kernel_size != 0)
@@ -290,7 +305,7 @@ at::Tensor gaussian_blur(const at::Tensor& images_in,
     const at::ScalarType out_type = dtype.value_or(images.scalar_type());
     at::Tensor out = at::empty(images.sizes(), images.options().dtype(out_type));
     DeviceContext& dc = context_for(images.device().index());
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     check(th_gaussian_blur(dc.ctx, images.data_ptr(), th_dtype_of(images.scalar_type()), images.size(0),
                            images.size(1), images.size(2), kernel_size, sigma, sparse ? 1 : 0, out.data_ptr(),
                            th_dtype_of(out_type), stream_of(images)),
@@ -346,7 +361,7 @@ std::tuple<at::Tensor, at::Tensor> marching_cubes(const at::Tensor& volume,
     a.unique_verts = unique_verts ? 1 : 0;
 
     DeviceContext& dc = context_for(volume.device().index());
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     void* stream = stream_of(volume);
     th_mc_info info{};
     check(th_marching_cubes(dc.ctx, &a, stream, &info), dc.ctx);
@@ -372,7 +387,7 @@ std::vector<std::tuple<at::Tensor, at::Tensor>> candidate_voxels_to_wireframes(
     at::cuda::CUDAGuard guard(candidate_voxels[0].device());
     const auto dev = candidate_voxels[0].device();
     DeviceContext& dc = context_for(dev.index());
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     void* stream = stream_of(candidate_voxels[0]);
     std::vector<std::tuple<at::Tensor, at::Tensor>> out;
     for (size_t i = 0; i < candidate_voxels.size(); ++i)
@@ -419,7 +434,7 @@ at::Tensor integral_image(const at::Tensor& masks_in)
     const at::Tensor masks = masks_in.contiguous();
     at::Tensor out = at::empty({ masks.size(0), masks.size(1), masks.size(2) }, masks.options().dtype(at::kFloat));
     DeviceContext& dc = context_for(masks.device().index());
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     check(th_integral_image(dc.ctx, masks.data_ptr(), th_dtype_of(masks.scalar_type()), masks.size(0), masks.size(1),
                             masks.size(2) * masks.size(3), out.data_ptr<float>(), stream_of(masks)),
           dc.ctx);
@@ -429,14 +444,14 @@ at::Tensor integral_image(const at::Tensor& masks_in)
 int64_t device_pool_bytes(int device)
 {
     DeviceContext& dc = context_for(device);
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     return th_context_device_bytes(dc.ctx);
 }
 
 void set_profiling(int device, bool enable)
 {
     DeviceContext& dc = context_for(device);
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     check(th_context_set_profiling(dc.ctx, enable ? 1 : 0), dc.ctx);
 }
 
@@ -444,7 +459,7 @@ void set_profiling(int device, bool enable)
 pybind11::dict stage_times(int device)
 {
     DeviceContext& dc = context_for(device);
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     th_stage_times t{};
     check(th_context_stage_times(dc.ctx, &t), dc.ctx);
     pybind11::dict d;
@@ -505,7 +520,7 @@ std::vector<std::tuple<at::Tensor, at::Tensor>> visual_hull_batch(const pybind11
     }
     at::cuda::CUDAGuard guard(keep[0].device());
     DeviceContext& dc = context_for(device);
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     void* stream = stream_of(keep[0]);
     std::vector<th_hull_info> infos(n);
     th_status st;
@@ -533,35 +548,35 @@ std::vector<std::tuple<at::Tensor, at::Tensor>> visual_hull_batch(const pybind11
 void set_carve_kernel(int device, int mode)
 {
     DeviceContext& dc = context_for(device);
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     check(th_context_set_option(dc.ctx, TH_OPTION_CARVE_KERNEL, mode), dc.ctx);
 }
 
 void set_graphs(int device, bool enable)
 {
     DeviceContext& dc = context_for(device);
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     check(th_context_set_option(dc.ctx, TH_OPTION_GRAPHS, enable ? 1 : 0), dc.ctx);
 }
 
 void set_batch_route(int device, bool enable)
 {
     DeviceContext& dc = context_for(device);
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     check(th_context_set_option(dc.ctx, TH_OPTION_BATCH_ROUTE, enable ? 1 : 0), dc.ctx);
 }
 
 void set_field_ones(int device, bool enable)
 {
     DeviceContext& dc = context_for(device);
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     check(th_context_set_option(dc.ctx, TH_OPTION_FIELD_ONES, enable ? 1 : 0), dc.ctx);
 }
 
 void set_field_masks(int device, bool enable)
 {
     DeviceContext& dc = context_for(device);
-    std::lock_guard<std::mutex> g(dc.lock);
+    auto g = lock_nogil(dc.lock);
     check(th_context_set_option(dc.ctx, TH_OPTION_FIELD_MASKS, enable ? 1 : 0), dc.ctx);
 }
 
@@ -602,7 +617,7 @@ public:
         th_hull_args a = hull_args(masks, transforms, level, cube_corner_bfl, cube_length, masks_partial,
                                    transforms_convention, unique_verts);
         void* stream = stream_of(masks);
-        std::lock_guard<std::mutex> g(lock_);
+        auto g = lock_nogil(lock_);
         th_hull_info info{};
         th_status st;
         {

@@ -1,10 +1,16 @@
 """Serving form: a continuous-batching request loop for visual hulls on one GPU.
 
-Requests (masks and transforms already on the device) are submitted at any
-time and return futures.  The server runs up to ``slots`` requests at once,
-each slot with its own resident context (SAT, octree and corner pools that
-stay allocated between requests) and its own CUDA stream, so the kernels of
-concurrent requests overlap on the device.  A request is admitted when a slot
+Requests are submitted at any time and return futures. Their masks and
+transforms may be on the device (the server's streams wait for the work the
+submitting thread had queued on its current stream when it called submit())
+or in host memory (copied in on the slot's stream, inside the measured
+latency; pinned memory makes the copy asynchronous). Host inputs must stay
+unchanged until the request's future resolves.
+
+The server runs up to ``slots`` requests at once, each slot with its own
+resident context (SAT, octree and corner pools that stay allocated between
+requests) and its own CUDA stream, so the kernels of concurrent requests
+overlap on the device.  A request is admitted when a slot
 is free and the device memory it needs fits in the admission budget together
 with the requests already running; otherwise it waits, and later requests
 that do fit may go first (no head-of-line blocking).  Every request's result
@@ -64,6 +70,8 @@ class _Job:
     future: concurrent.futures.Future
     arrival: float
     bytes: int
+    ready: torch.cuda.Event | None  # recorded on the submitter's stream (device inputs)
+    consumer: torch.cuda.Stream  # the submitter's current stream, where the results will be used
     started: float = 0.0
 
 
@@ -101,15 +109,25 @@ class HullServer:
 
     # -- client side ---------------------------------------------------------
     def submit(self, req: HullRequest) -> concurrent.futures.Future:
-        """Queues a request; the future resolves to (verts, faces) on the device."""
+        """Queues a request; the future resolves to (verts, faces) on the device.
+
+        The results are complete when the future resolves and may be used on
+        the stream that was current in the submitting thread (the server
+        records that use with the caching allocator); other streams must
+        synchronise with it first."""
         need = estimate_bytes(req)
         if need > self.budget:
             raise ValueError(f"request needs {need} bytes, more than the admission budget {self.budget}")
         fut: concurrent.futures.Future = concurrent.futures.Future()
+        consumer = torch.cuda.current_stream(self.device)
+        ready = None
+        if req.masks.is_cuda or req.transforms.is_cuda:
+            ready = torch.cuda.Event()
+            ready.record(consumer)
         with self._cv:
             if self._closed:
                 raise RuntimeError("server is closed")
-            self._pending.append(_Job(req, fut, time.perf_counter(), need))
+            self._pending.append(_Job(req, fut, time.perf_counter(), need, ready, consumer))
             self._cv.notify_all()
         return fut
 
@@ -182,8 +200,15 @@ class HullServer:
             try:
                 r = job.req
                 with torch.cuda.stream(stream):
-                    verts, faces = ctx.visual_hull(r.masks, r.transforms, r.level, r.cube_corner_bfl, r.cube_length,
+                    if job.ready is not None:
+                        stream.wait_event(job.ready)
+                    masks = r.masks.to(self.device, non_blocking=True)
+                    transforms = r.transforms.to(self.device, non_blocking=True)
+                    verts, faces = ctx.visual_hull(masks, transforms, r.level, r.cube_corner_bfl, r.cube_length,
                                                    r.masks_partial, r.transforms_convention, r.unique_verts)
+                    if job.consumer != stream:
+                        verts.record_stream(job.consumer)
+                        faces.record_stream(job.consumer)
                 stream.synchronize()
                 done = time.perf_counter()
                 job.future.set_result((verts, faces))
