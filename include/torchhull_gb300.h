@@ -324,7 +324,11 @@ typedef enum th_option
      * level's cells (levels 1 to 10) tell the field which (corner, view)
      * factors are exactly 1, and it skips them; 0: every pair is evaluated.
      * Results are identical. */
-    TH_OPTION_FIELD_MASKS = 5
+    TH_OPTION_FIELD_MASKS = 5,
+    /* 1 (default): integral images of 0/1 masks (H*W <= 2^24, W <= 4096) are
+     * built in one banded pass (exact integer sums, any order); 0: always the
+     * two sequential passes in torch's addition order.  Results are identical. */
+    TH_OPTION_SAT_SINGLE_PASS = 6
 } th_option;
 th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value);
 th_status th_context_stage_times(const th_context* ctx, th_stage_times* out);

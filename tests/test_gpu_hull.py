@@ -121,6 +121,66 @@ def test_integral_image_bitwise(th, cuda, dtype):
     assert np.array_equal(sat.view(np.uint32), ref_torch.view(np.uint32))
 
 
+def _cumsum_sat(masks):
+    return torch.cumsum(torch.cumsum(masks, 1, dtype=torch.float32), 2, dtype=torch.float32)[..., 0]
+
+
+@pytest.mark.parametrize("shape", [(32, 1024, 1024), (3, 97, 131), (2, 256, 256), (4, 512, 768), (2, 1000, 1000),
+                                   (1, 1024, 2048), (1, 33, 4096), (5, 17, 1)])
+@pytest.mark.parametrize("dtype", [torch.uint8, torch.float16, torch.float32, torch.float64])
+def test_integral_image_binary_shapes(th, cuda, shape, dtype):
+    """0/1 masks take the single pass (banded, look-back carries): equal to torch's cumsum on the device."""
+    g = torch.Generator(device=cuda).manual_seed(sum(shape))
+    B, H, W = shape
+    # a blob plus noise: long runs of ones and zeros, and isolated pixels
+    yy, xx = torch.meshgrid(torch.arange(H, device=cuda), torch.arange(W, device=cuda), indexing="ij")
+    blob = ((yy - H / 2) ** 2 + (xx - W / 3) ** 2) < (0.3 * max(H, W)) ** 2
+    noise = torch.rand((B, H, W), generator=g, device=cuda) < 0.02
+    masks = (blob[None] ^ noise).to(dtype)[..., None].contiguous()
+    ref = _cumsum_sat(masks)
+    assert torch.equal(th.integral_image(masks).view(torch.int32), ref.view(torch.int32))
+    # twice: the band scratch (tickets, status words) must come back clean
+    assert torch.equal(th.integral_image(masks).view(torch.int32), ref.view(torch.int32))
+
+
+def test_integral_image_shape_sequence(th, cuda):
+    """Calls of different shapes in a row share one scratch whose layout depends on the shape."""
+    g = torch.Generator(device=cuda).manual_seed(9)
+    for shape in [(16, 1024, 1024), (6, 128, 128), (16, 1024, 1024), (3, 512, 256), (8, 1024, 768)]:
+        masks = (torch.rand(shape + (1,), generator=g, device=cuda) < 0.85).float()
+        assert torch.equal(th.integral_image(masks).view(torch.int32), _cumsum_sat(masks).view(torch.int32)), shape
+
+
+@pytest.mark.parametrize("offset", [1, 3])
+def test_integral_image_unaligned_masks(th, cuda, offset):
+    """Masks starting off a 16-byte boundary are staged without the bulk copy."""
+    base = (torch.rand((2 * 256 * 256 + offset,), device=cuda) < 0.5).to(torch.uint8)
+    masks = base[offset:].view(2, 256, 256, 1)
+    assert torch.equal(th.integral_image(masks).view(torch.int32), _cumsum_sat(masks).view(torch.int32))
+
+
+def test_integral_image_nonbinary_falls_back(th, cuda):
+    """A value other than 0/1 anywhere: the exact sequential passes rebuild the whole table."""
+    masks = (torch.rand((4, 512, 512, 1), device=cuda) < 0.5).float()
+    masks[2, 300, 17, 0] = 0.25
+    assert torch.equal(th.integral_image(masks).view(torch.int32), _cumsum_sat(masks).view(torch.int32))
+    binary = (masks > 0.5).float()
+    assert torch.equal(th.integral_image(binary).view(torch.int32), _cumsum_sat(binary).view(torch.int32))
+
+
+@pytest.mark.parametrize("single_pass", [True, False])
+def test_sat_option_gives_identical_hulls(th, cuda, single_pass):
+    """TH_OPTION_SAT_SINGLE_PASS changes how the integral image is built, not the result."""
+    r = scenes.make_request(542, 16, 1024, 8, True, device=cuda)
+    want = th.visual_hull(**r.kwargs())
+    try:
+        th._C.set_sat_single_pass(0, single_pass)
+        got = th.visual_hull(**r.kwargs())
+    finally:
+        th._C.set_sat_single_pass(0, True)
+    assert torch.equal(got[1], want[1]) and torch.equal(got[0].view(torch.int32), want[0].view(torch.int32))
+
+
 def test_arithmetic_probe(cuda):
     """The oracle's float->int64 and fused world-coordinate rules hold on the device."""
     import ctypes

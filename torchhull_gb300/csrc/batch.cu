@@ -60,17 +60,22 @@ __device__ __forceinline__ ItemResult batch_item(const BatchReq& q,
                                                  bool want_skip,
                                                  bool skip_inside,
                                                  bool want_out,
-                                                 int grow)
+                                                 int grow,
+                                                 bool want_inside)
 {
     const ViewSource src = make_view_source(q.tf, q.sat, q.H, q.W);
     if constexpr (VARIANT >= 0)
         return classify_item<(VARIANT >> 1) != 0, (VARIANT & 1) != 0>(src, b, wx, wy, wz, want_skip, skip_inside,
-                                                                      want_out, grow);
+                                                                      want_out, grow, want_inside);
     if (q.partial)
-        return q.opengl ? classify_item<true, true>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow)
-                        : classify_item<true, false>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow);
-    return q.opengl ? classify_item<false, true>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow)
-                    : classify_item<false, false>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow);
+        return q.opengl ? classify_item<true, true>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow,
+                                                    want_inside)
+                        : classify_item<true, false>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow,
+                                                     want_inside);
+    return q.opengl ? classify_item<false, true>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow,
+                                                 want_inside)
+                    : classify_item<false, false>(src, b, wx, wy, wz, want_skip, skip_inside, want_out, grow,
+                                                  want_inside);
 }
 
 // Entries of level li that were written (a pool overflow drops the rest).
@@ -163,37 +168,23 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 2) batch_carve_kernel(BatchP
                     const bool skip_inside = qq.partial != 0;
                     const bool want_out = qq.partial && (li + 1 < qq.level) && b < 32;
                     const int grow = li + 2 == qq.level ? 1 : 2;
-                    res = batch_item<VARIANT>(qq, b, wx, wy, wz, produce && b < 32, skip_inside, want_out, grow);
+                    res = batch_item<VARIANT>(qq, b, wx, wy, wz, produce && b < 32, skip_inside, want_out, grow,
+                                              li + 1 == qq.level);
                     if (res.out == 0xffu)
                         atomicOr(&ws.cout_all[s], 1u << b);
                     else
                         for (uint32_t o = res.out; o; o &= o - 1)
                             atomicOr(&ws.cout[s][__ffs(o) - 1], 1u << b);
-                }
-                const int seg = act ? s : -1 - lane;
-                const int prev_seg = __shfl_up_sync(0xffffffffu, seg, 1);
-                const bool head = act && (lane == 0 || prev_seg != seg);
-                const uint32_t e_or = run_or(res.empty, seg, lane);
-                const uint32_t r_or = run_or(res.refine, seg, lane);
-                const uint32_t i_or = run_or(res.inside, seg, lane);
-                if (head)
-                {
-                    if (e_or)
-                        atomicOr(&ws.empty[s], e_or);
-                    if (r_or)
-                        atomicOr(&ws.refine[s], r_or);
-                    if (i_or)
-                        atomicOr(&ws.inside[s], i_or);
-                }
-                if (__any_sync(0xffffffffu, produce))
-                {
-#pragma unroll
-                    for (int c = 0; c < 8; ++c)
-                    {
-                        const uint32_t v = run_or(((res.skip >> c) & 1u) << (b & 31), seg, lane);
-                        if (head && v)
-                            atomicOr(&ws.cskip[s][c], v);
-                    }
+                    // merge into the slot's words: one shared atomic per non-zero word
+                    if (res.empty)
+                        atomicOr(&ws.empty[s], res.empty);
+                    if (res.refine)
+                        atomicOr(&ws.refine[s], res.refine);
+                    if (res.inside)
+                        atomicOr(&ws.inside[s], res.inside);
+                    if (produce)
+                        for (uint32_t m = res.skip; m; m &= m - 1)
+                            atomicOr(&ws.cskip[s][__ffs(m) - 1], 1u << (b & 31));
                 }
             }
             __syncwarp();

@@ -125,7 +125,7 @@ bool is_image_dtype(int d)
 struct HullSlot
 {
     DevBuf tf, sat, ones, cell_masks, nodes, node_skip, node_out, child_masks, child_skip, child_out, tile_sums, bitmap,
-            word_rank, rowbits, rows, corners, values, codes, emask, soup_off, vbase, counters, flags;
+            word_rank, rowbits, rows, corners, values, codes, emask, soup_off, vbase, counters, flags, sat_scratch;
     int64_t node_cap = 0, corner_cap = 0, parent_cap = 0;
     HullPlan plan{};
     DevCounters* host = nullptr; // pinned copy of the counters
@@ -158,7 +158,7 @@ struct HullSlot
     {
         return { &tf,     &sat,  &ones,  &cell_masks,   &nodes,     &node_skip,   &node_out,  &child_masks, &child_skip, &child_out, &tile_sums,
                  &bitmap, &word_rank, &rowbits, &rows, &corners,    &values,     &codes,
-                 &emask,  &soup_off, &vbase,   &counters, &flags, &rq };
+                 &emask,  &soup_off, &vbase,   &counters, &flags, &sat_scratch, &rq };
     }
 
     void release()
@@ -344,6 +344,8 @@ struct th_context
     th::BatchState bstate;
     th::DevBuf blur_scratch;
     th::DevBuf blurred; // masks blurred by th_visual_hull_blurred
+    th::DevBuf sat_aux; // th_integral_image: its 0/1 flag word, then the single pass's scratch
+    cudaEvent_t sat_aux_done = nullptr; // the last th_integral_image that used sat_aux
     th::McSlot mc;
     bool profiling = false;
     th::StageEvents events;
@@ -353,6 +355,7 @@ struct th_context
     bool batch_route = false; // TH_OPTION_BATCH_ROUTE
     bool field_ones = true;   // TH_OPTION_FIELD_ONES
     bool field_masks = true;  // TH_OPTION_FIELD_MASKS
+    bool sat_single_pass = true; // TH_OPTION_SAT_SINGLE_PASS
     std::map<th::TuneKey, th::CarveVariants> carve_tuned;
     cudaEvent_t tune_ev[2] = { nullptr, nullptr };
 };
@@ -371,7 +374,7 @@ int64_t pool_bytes(const th_context* ctx)
         return b;
     };
     int64_t total = sum(ctx->hull) + static_cast<int64_t>(ctx->blur_scratch.bytes) +
-                    static_cast<int64_t>(ctx->blurred.bytes);
+                    static_cast<int64_t>(ctx->blurred.bytes) + static_cast<int64_t>(ctx->sat_aux.bytes);
     for (const DevBuf* d : ctx->mc.buffers())
         total += static_cast<int64_t>(d->bytes);
     for (const auto& s : ctx->batch)
@@ -454,6 +457,9 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_one
 
     s.tf.ensure(sizeof(float) * std::max<int64_t>(B, 1) * 16);
     s.sat.ensure(sizeof(float) * std::max<int64_t>(B * H * W, 1));
+    const int64_t sat_scratch = sat_scratch_bytes(B, H, W, a->masks_dtype);
+    if (sat_scratch > 0)
+        s.sat_scratch.ensure(static_cast<size_t>(sat_scratch));
     const int64_t WW = (W + 31) / 32;
     // the field's cell-mask table of level L-1 (up to 2^27 cells, 512 MB:
     // level 10) skips most pairs; the all-ones bitmap only pays without it
@@ -705,7 +711,8 @@ void run_hull_once(th_context* ctx,
             launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), st);
             TH_CUDA(cudaMemsetAsync(s.flags.p, 0, sizeof(unsigned int), st));
             launch_integral_image(a->masks, a->masks_dtype, a->batch, a->height, a->width, s.sat.as<float>(), st,
-                                  s.flags.as<unsigned int>());
+                                  s.flags.as<unsigned int>(),
+                                  ctx->sat_single_pass ? SatScratch{ s.sat_scratch.p } : SatScratch{});
             if (ev)
                 ev->record(1, st);
         }
@@ -906,7 +913,8 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
                 launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), sr);
                 TH_CUDA(cudaMemsetAsync(s.flags.p, 0, sizeof(unsigned int), sr));
                 launch_integral_image(a->masks, a->masks_dtype, a->batch, a->height, a->width, s.sat.as<float>(), sr,
-                                      s.flags.as<unsigned int>());
+                                      s.flags.as<unsigned int>(),
+                                      ctx->sat_single_pass ? SatScratch{ s.sat_scratch.p } : SatScratch{});
             }
             for (int i = 0; i < nstreams; ++i)
             {
@@ -1307,6 +1315,9 @@ void th_context_destroy(th_context* ctx)
         s.release();
     ctx->blur_scratch.release();
     ctx->blurred.release();
+    ctx->sat_aux.release();
+    if (ctx->sat_aux_done)
+        cudaEventDestroy(ctx->sat_aux_done);
     ctx->mc.release();
     ctx->bstate.release();
     ctx->events.destroy();
@@ -1362,6 +1373,8 @@ th_status th_context_set_option(th_context* ctx, int32_t option, int64_t value)
             ctx->field_ones = value != 0;
         else if (option == TH_OPTION_FIELD_MASKS && (value == 0 || value == 1))
             ctx->field_masks = value != 0;
+        else if (option == TH_OPTION_SAT_SINGLE_PASS && (value == 0 || value == 1))
+            ctx->sat_single_pass = value != 0;
         else
             throw ArgError{ TH_ERR_INVALID_ARGUMENT, "unknown option or value" };
     });
@@ -1537,7 +1550,26 @@ th_status th_integral_image(th_context* ctx,
             return;
         if (!masks || !out)
             throw ArgError{ TH_ERR_INVALID_ARGUMENT, "masks or out pointer is NULL" };
-        launch_integral_image(masks, masks_dtype, batch, height, width, out, static_cast<cudaStream_t>(stream));
+        const cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const int64_t sb = ctx->sat_single_pass ? sat_scratch_bytes(batch, height, width, masks_dtype) : 0;
+        unsigned int* flag = nullptr;
+        SatScratch sc{};
+        if (sb > 0)
+        {
+            constexpr int64_t kFlagBytes = 256;
+            // calls on different streams share sat_aux: each waits for the previous one
+            if (!ctx->sat_aux_done)
+                TH_CUDA(cudaEventCreateWithFlags(&ctx->sat_aux_done, cudaEventDisableTiming));
+            else
+                TH_CUDA(cudaStreamWaitEvent(st, ctx->sat_aux_done, 0));
+            ctx->sat_aux.ensure(static_cast<size_t>(kFlagBytes + sb));
+            flag = ctx->sat_aux.as<unsigned int>();
+            TH_CUDA(cudaMemsetAsync(flag, 0, sizeof(unsigned int), st));
+            sc = SatScratch{ static_cast<unsigned char*>(ctx->sat_aux.p) + kFlagBytes };
+        }
+        launch_integral_image(masks, masks_dtype, batch, height, width, out, st, flag, sc);
+        if (sb > 0)
+            TH_CUDA(cudaEventRecord(ctx->sat_aux_done, st));
     });
 }
 

@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_views_kernel
             for (int64_t b = sub; b < p.B; b += LANES)
             {
                 const ItemResult r = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, produce, L.skip_inside,
-                                                                    produce_out, L.skip_grow);
+                                                                    produce_out, L.skip_grow, L.last);
                 empty |= r.empty;
                 refine |= r.refine;
                 inside |= r.inside;
@@ -285,37 +285,24 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) classify_items_kernel
                 lattice_world(p.rq->corner, p.rq->length, is, li, L.inv_rc, wx, wy, wz);
                 const ViewSource src = make_view_source(p.tf, p.sat, p.H, p.W);
                 res = classify_item<PARTIAL, OPENGL>(src, b, wx, wy, wz, L.produce && b < 32, L.skip_inside,
-                                                     L.produce_out && b < 32, L.skip_grow);
+                                                     L.produce_out && b < 32, L.skip_grow, L.last);
                 if (res.out == 0xffu)
                     atomicOr(&ws.cout_all[s], 1u << b);
                 else
                     for (uint32_t o = res.out; o; o &= o - 1)
                         atomicOr(&ws.cout[s][__ffs(o) - 1], 1u << b);
-            }
-            const int seg = act ? s : -1 - lane;
-            const int prev_seg = __shfl_up_sync(0xffffffffu, seg, 1);
-            const bool head = act && (lane == 0 || prev_seg != seg);
-            const uint32_t e_or = run_or(res.empty, seg, lane);
-            const uint32_t r_or = run_or(res.refine, seg, lane);
-            const uint32_t i_or = run_or(res.inside, seg, lane);
-            if (head)
-            {
-                if (e_or)
-                    atomicOr(&ws.empty[s], e_or);
-                if (r_or)
-                    atomicOr(&ws.refine[s], r_or);
-                if (i_or)
-                    atomicOr(&ws.inside[s], i_or);
-            }
-            if (L.produce)
-            {
-#pragma unroll
-                for (int c = 0; c < 8; ++c)
-                {
-                    const uint32_t v = run_or(((res.skip >> c) & 1u) << (b & 31), seg, lane);
-                    if (head && v)
-                        atomicOr(&ws.cskip[s][c], v);
-                }
+                // merge into the slot's words: one shared atomic per non-zero
+                // word (a slot's items sit in neighbouring lanes, so conflicts
+                // are short)
+                if (res.empty)
+                    atomicOr(&ws.empty[s], res.empty);
+                if (res.refine)
+                    atomicOr(&ws.refine[s], res.refine);
+                if (res.inside)
+                    atomicOr(&ws.inside[s], res.inside);
+                if (L.produce)
+                    for (uint32_t m = res.skip; m; m &= m - 1)
+                        atomicOr(&ws.cskip[s][__ffs(m) - 1], 1u << (b & 31));
             }
         }
         __syncwarp();

@@ -187,21 +187,6 @@ __device__ __forceinline__ int select_bit(uint32_t m, int j)
     return __ffs(m) - 1;
 }
 
-// OR of v over the run of lanes with the same slot s (slots ascend over the
-// lanes); the run's first lane returns the full OR.
-__device__ __forceinline__ uint32_t run_or(uint32_t v, int s, int lane)
-{
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1)
-    {
-        const uint32_t vo = __shfl_down_sync(0xffffffffu, v, d);
-        const int so = __shfl_down_sync(0xffffffffu, s, d);
-        if (lane + d < 32 && so == s)
-            v |= vo;
-    }
-    return v;
-}
-
 // World coordinates of the lattice of the cell idx (ravelled at resolution
 // 2^li): c + v/r * L with the product fused (visual_hull_cuda.cu:206-213);
 // v/r == v * (1/r) exactly (r = 2^k).
@@ -247,7 +232,15 @@ __device__ __forceinline__ ViewSource make_view_source(const float* tf, const fl
 // mode): compute the children's out-of-frame bits (box_out); grow: the skip
 // rule's margin in pixels, 2 for masks inherited by all descendants, 1 for the
 // children whose own children are leaves (one level below them, and the
-// field's bilinear footprints of the leaves' corners, stay within one pixel).
+// field's bilinear footprints of the leaves' corners, stay within one pixel);
+// want_inside (partial mode): compute the children's "fully inside" bits (only
+// the last level uses them).
+//
+// "Every corner rounds into the frame" (a pixel coordinate q passes when
+// 0.5 <= q < size - 1.5, NaN fails) is tested on the child's box: for corners
+// without NaN it holds for all eight exactly when it holds for the box's
+// minimum and maximum, so the box test plus a NaN bit per lattice point gives
+// the per-corner answer (fminf/fmaxf leave NaN out of the box).
 template <bool PARTIAL, bool OPENGL>
 __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                                                     int64_t b,
@@ -257,7 +250,8 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                                                     bool want_skip,
                                                     bool skip_inside,
                                                     bool want_out = false,
-                                                    int grow = 2)
+                                                    int grow = 2,
+                                                    bool want_inside = true)
 {
     const int32_t H = static_cast<int32_t>(p.H), W = static_cast<int32_t>(p.W);
     const float Hf = p.Hf, Wf = p.Wf;
@@ -271,8 +265,11 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
     const float in2_hx = __fsub_rn(Wf, 2.5f), in2_hy = __fsub_rn(Hf, 2.5f);
     ItemResult out{ 0, 0, 0, 0, 0 };
     want_out = PARTIAL && want_out;
+    want_inside = PARTIAL && want_inside;
+    const bool want_in2 = PARTIAL && want_skip && skip_inside;
+    const bool want_nan = want_inside || want_in2;
     Box prev[4];
-    uint32_t prev_in = 0, prev_in2 = 0, prev_front = 0;
+    uint32_t prev_nan = 0, prev_front = 0;
     // Rolled (the default), the plane loop keeps one copy of the plane's code,
     // a third of the unrolled footprint: 9-11 % faster carve levels on GB300
     // (fewer instruction-fetch stalls); unrolled, it schedules across planes.
@@ -288,7 +285,7 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
         const float tzy = __fmaf_rn(ry.z, wzz, ry.w);
         const float tzd = __fmaf_rn(rd.z, wzz, rd.w);
         float px[9], py[9];
-        uint32_t in9 = 0, in9b = 0, front9 = 0;
+        uint32_t nan9 = 0, front9 = 0;
 #pragma unroll
         for (int y = 0; y < 3; ++y)
         {
@@ -317,19 +314,12 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                 }
                 if ((want_skip || want_out) && cd > 0.f)
                     front9 |= 1u << k;
-                if (PARTIAL)
-                {
-                    // 1 <= round(q) < size - 1 (round half away from zero)
-                    // exactly when 0.5 <= q < size - 1.5; NaN fails both
-                    if (px[k] >= 0.5f && px[k] < in_hx && py[k] >= 0.5f && py[k] < in_hy)
-                        in9 |= 1u << k;
-                    if (skip_inside && px[k] >= 1.5f && px[k] < in2_hx && py[k] >= 1.5f && py[k] < in2_hy)
-                        in9b |= 1u << k;
-                }
+                if (want_nan && !(px[k] == px[k] && py[k] == py[k]))
+                    nan9 |= 1u << k;
             }
         }
         Box cur[4];
-        uint32_t cur_in = 0, cur_in2 = 0, cur_front = 0;
+        uint32_t cur_nan = 0, cur_front = 0;
 #pragma unroll
         for (int c = 0; c < 4; ++c)
         {
@@ -340,10 +330,8 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                           fmaxf(fmaxf(px[k0], px[k1]), fmaxf(px[k2], px[k3])),
                           fmaxf(fmaxf(py[k0], py[k1]), fmaxf(py[k2], py[k3])) };
             const uint32_t need = (1u << k0) | (1u << k1) | (1u << k2) | (1u << k3);
-            if ((in9 & need) == need)
-                cur_in |= 1u << c;
-            if ((in9b & need) == need)
-                cur_in2 |= 1u << c;
+            if (nan9 & need)
+                cur_nan |= 1u << c;
             if ((front9 & need) == need)
                 cur_front |= 1u << c;
         }
@@ -355,8 +343,12 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                 const uint32_t cbit = 1u << c;
                 const uint32_t bit = 1u << (c + 4 * (z - 1));
                 const bool front = (prev_front & cur_front & cbit) != 0;
-                const bool in2 = (prev_in2 & cur_in2 & cbit) != 0;
+                const bool nan = ((prev_nan | cur_nan) & cbit) != 0;
                 const Box cb = merge(prev[c], cur[c]);
+                // 1 <= round(q) < size - 1 (round half away from zero) exactly
+                // when 0.5 <= q < size - 1.5; two pixels in: 1.5 <= q < size - 2.5
+                const bool in2 = want_in2 && !nan && cb.minx >= 1.5f && cb.maxx < in2_hx && cb.miny >= 1.5f &&
+                                 cb.maxy < in2_hy;
                 const ViewResult r = classify_view<PARTIAL>(sat_b, H, W, Hf, Wf, cb,
                                                             want_skip && front && (!skip_inside || in2), grow);
                 if (want_out && front && box_out(cb, Hf, Wf))
@@ -367,15 +359,15 @@ __device__ __forceinline__ ItemResult classify_item(const ViewSource& p,
                     out.refine |= bit;
                 if (r.skip)
                     out.skip |= bit;
-                if (PARTIAL && (prev_in & cur_in & cbit))
+                if (want_inside && !nan && cb.minx >= 0.5f && cb.maxx < in_hx && cb.miny >= 0.5f &&
+                    cb.maxy < in_hy)
                     out.inside |= bit;
             }
         }
 #pragma unroll
         for (int c = 0; c < 4; ++c)
             prev[c] = cur[c];
-        prev_in = cur_in;
-        prev_in2 = cur_in2;
+        prev_nan = cur_nan;
         prev_front = cur_front;
     }
     return out;

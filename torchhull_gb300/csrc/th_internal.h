@@ -46,8 +46,20 @@ int sm_count();
 // cover the work, at most 8 resident blocks per SM.
 int grid_for(int64_t work_items, int threads);
 
+// Scratch of the single-pass integral image (sat.cu): device memory of at
+// least sat_scratch_bytes(B, H, W, dtype) bytes (each launch clears what it needs).
+struct SatScratch
+{
+    void* p = nullptr;
+};
+
+// Bytes of scratch the single pass needs, 0 when it does not apply.
+int64_t sat_scratch_bytes(int64_t B, int64_t H, int64_t W, int dtype);
+
 // Integral image (sat.cu).  masks [B,H,W] of dtype, out [B,H,W] float32.
-// nonbinary (optional, zeroed by the caller) is set to 1 if any mask value is neither 0 nor 1.
+// nonbinary (optional, zeroed by the caller) is set non-zero if any mask value
+// is neither 0 nor 1.  With scratch and nonbinary, 0/1 masks take the single
+// pass; otherwise (and after it, gated on the device) the exact two passes.
 void launch_integral_image(const void* masks,
                            int dtype,
                            int64_t B,
@@ -55,7 +67,8 @@ void launch_integral_image(const void* masks,
                            int64_t W,
                            float* out,
                            cudaStream_t s,
-                           unsigned int* nonbinary = nullptr);
+                           unsigned int* nonbinary = nullptr,
+                           SatScratch scratch = {});
 
 // Transform conversion to float32 row-major [B,16] (sat.cu).
 void launch_convert_transforms(const void* tf, int dtype, int64_t B, float* out, cudaStream_t s);

@@ -573,6 +573,13 @@ void set_field_ones(int device, bool enable)
     check(th_context_set_option(dc.ctx, TH_OPTION_FIELD_ONES, enable ? 1 : 0), dc.ctx);
 }
 
+void set_sat_single_pass(int device, bool enable)
+{
+    DeviceContext& dc = context_for(device);
+    auto g = lock_nogil(dc.lock);
+    check(th_context_set_option(dc.ctx, TH_OPTION_SAT_SINGLE_PASS, enable ? 1 : 0), dc.ctx);
+}
+
 void set_field_masks(int device, bool enable)
 {
     DeviceContext& dc = context_for(device);
@@ -689,6 +696,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
           "Field: skip the mask reads of samples whose 2x2 footprint is all ones (default on).");
     m.def("set_field_masks", &set_field_masks, "device"_a, "enable"_a,
           "Field: skip the (corner, view) pairs whose factor the carve proved to be 1 (default on).");
+    m.def("set_sat_single_pass", &set_sat_single_pass, "device"_a, "enable"_a,
+          "Integral images of 0/1 masks in one banded pass (default on).");
     m.def("set_graphs", &set_graphs, "device"_a, "enable"_a,
           "Replay each request shape's pipeline as a captured CUDA graph (default on).");
     pybind11::class_<HullContext>(m, "HullContext", "Context with its own device pools (one request at a time).")
