@@ -336,12 +336,6 @@ th_status th_context_stage_times(const th_context* ctx, th_stage_times* out);
 /* Number of kernels this library has launched in this process (all contexts). */
 int64_t th_launch_count(void);
 
-/* Diagnostics (no reference counterpart): evaluates the device arithmetic the
- * oracle emulates: out_i64[i] = (int64) in[i] as the GPU converts it, and
- * out_f32[i] = c + v[i]/r * L written as the reference writes it. */
-th_status th_probe_arithmetic(const float* in, int64_t* out_i64, int64_t n, const int64_t* v, float r, float c, float L,
-                              float* out_f32, void* stream);
-
 #ifdef __cplusplus
 }
 #endif

@@ -185,19 +185,19 @@ def test_arithmetic_probe(cuda):
     """The oracle's float->int64 and fused world-coordinate rules hold on the device."""
     import ctypes
 
-    from torchhull_gb300 import build
+    from tests.probe import build_probe
 
-    lib = ctypes.CDLL(str(build.LIB))
+    lib = ctypes.CDLL(str(build_probe.build()))
     vals = torch.tensor([float("nan"), float("inf"), -float("inf"), 3e38, -3e38, 9.3e18, -9.3e18, 2.5, -2.5, 1e10],
                         dtype=torch.float32, device=cuda)
     out = torch.empty(vals.numel(), dtype=torch.int64, device=cuda)
     v = torch.arange(vals.numel(), dtype=torch.int64, device=cuda) * 37 + 5
     fo = torch.empty(vals.numel(), dtype=torch.float32, device=cuda)
-    lib.th_probe_arithmetic.restype = ctypes.c_int
-    lib.th_probe_arithmetic.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+    lib.probe_arithmetic.restype = ctypes.c_int
+    lib.probe_arithmetic.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_void_p,
                                         ctypes.c_void_p]
-    rc = lib.th_probe_arithmetic(vals.data_ptr(), out.data_ptr(), vals.numel(), v.data_ptr(), 512.0, -1.1, 2.2,
+    rc = lib.probe_arithmetic(vals.data_ptr(), out.data_ptr(), vals.numel(), v.data_ptr(), 512.0, -1.1, 2.2,
                                  fo.data_ptr(), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     torch.cuda.synchronize()
     assert rc == 0

@@ -26,7 +26,7 @@ OBJ = BUILD / "obj"
 EXT_DIR = BUILD / "ext"
 LIB = BUILD / "libtorchhull_gb300.so"
 EXT_NAME = "torchhull_gb300_C"
-CU_SOURCES = ["sat.cu", "carve.cu", "batch.cu", "mesh.cu", "mc.cu", "wire.cu", "blur.cu", "blur_noalloc.cu", "capi.cu", "probe.cu"]
+CU_SOURCES = ["sat.cu", "carve.cu", "batch.cu", "mesh.cu", "mc.cu", "wire.cu", "blur.cu", "blur_noalloc.cu", "capi.cu"]
 HEADERS = ["th_common.cuh", "th_hull.cuh", "th_classify.cuh", "th_batch.cuh", "th_mc.cuh", "th_internal.h", "mc_tables.h"]
 
 NVCC_FLAGS = [
