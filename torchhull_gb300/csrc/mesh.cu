@@ -843,61 +843,118 @@ __global__ void __launch_bounds__(32 * kExportWarps) export_faces_kernel(HullPla
     }
 }
 
-// Unique vertices: vertices and faces in one pass.  A warp takes 32
-// consecutive corners; their vertices (one per set edge bit, numbered by
-// vbase) and their cells' face entries (numbered by soup_off) are two
-// contiguous output ranges, each dealt out one entry per lane and stored
-// coalesced.  The +x neighbour of a vertex edge is the next corner rank; the
-// faces look their corners' ranks up once per cell (cell_ranks).
+// Unique vertices: vertices and faces in one pass.  A warp takes 128
+// consecutive corners at a time: their data (code, edge bits, id, value) is
+// staged in shared memory with coalesced loads, and their vertices (one per
+// set edge bit, numbered by vbase) and face entries (numbered by soup_off)
+// form two contiguous output ranges, dealt out one entry per lane (the owner
+// of entry k is found by a binary search over the staged prefix sums), so the
+// rank and value gathers run on all lanes although only about a quarter of
+// the corners own any vertex or face.  The +x neighbour of a corner of the
+// mesh has the next rank; other neighbours are looked up in the bitmap.
+// Face columns 1 and 2 are swapped as flip_faces does
+// (visual_hull_cuda.cu:941-956): entry k of a triangle goes to k's mirror.
+constexpr int kExportPer = 4;                   // corners per lane
+constexpr int kExportChunk = 32 * kExportPer;   // corners per warp and iteration
+
+struct ExportStage
+{
+    int64_t id[kExportChunk];
+    float val[kExportChunk];
+    int32_t vpre[kExportChunk]; // exclusive prefix of the vertex counts over the chunk
+    int32_t fpre[kExportChunk]; // exclusive prefix of the face-entry counts
+    uint8_t code[kExportChunk], em[kExportChunk], nv[kExportChunk], nf[kExportChunk];
+};
+
+// Largest c in [0, kExportChunk) with pre[c] <= k (pre non-decreasing, pre[0] = 0).
+__device__ __forceinline__ int stage_owner(const int32_t* pre, int k)
+{
+    int c = 0;
+#pragma unroll
+    for (int step = kExportChunk / 2; step > 0; step >>= 1)
+        if (pre[c + step] <= k)
+            c += step;
+    return c;
+}
+
 __global__ void __launch_bounds__(32 * kExportWarps) export_mesh_kernel(HullPlan p, float* __restrict__ verts, int64_t* __restrict__ faces)
 {
     __shared__ TableCache tab;
-    __shared__ int64_t stage_all[kExportWarps][32 * 15];
-    __shared__ uint32_t ranks_all[kExportWarps][32][9];
+    __shared__ ExportStage stage_all[kExportWarps];
     load_tables(tab);
-    int64_t* stage = stage_all[threadIdx.x >> 5];
-    uint32_t(*ranks)[9] = ranks_all[threadIdx.x >> 5];
+    __syncthreads();
+    ExportStage& st = stage_all[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const int64_t n = p.ctr->corners;
     const float scale = __fdiv_rn(p.length, static_cast<float>(int64_t{ 1 } << p.level));
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-    for (int64_t wb = warp * 32; wb < n; wb += nwarps * 32)
+    for (int64_t wb = warp * kExportChunk; wb < n; wb += nwarps * kExportChunk)
     {
-        const int64_t t = wb + lane;
-        const bool valid = t < n;
-        const uint32_t code = valid ? p.codes[t] : 0u;
-        const int cnt = tab.count[code];
-        const uint32_t bits = valid ? p.emask[t] : 0u;
-        const int nvert = __popc(bits);
-        if (!__any_sync(0xffffffffu, cnt > 0 || nvert > 0))
-            continue;
-        const int64_t id = (cnt > 0 || nvert > 0) ? p.corners[t] : 0;
-
-        // vertices: the warp's range starts at lane 0's vertex base
-        const int64_t vlo = __shfl_sync(0xffffffffu, valid ? static_cast<int64_t>(p.vbase[t]) : int64_t{ 0 }, 0);
-        const float v1 = nvert ? p.values[t] : 0.f;
-        const int vincl = warp_inclusive_scan(nvert);
-        const int vexcl = vincl - nvert;
-        const int vtot = __shfl_sync(0xffffffffu, vincl, 31);
-        for (int k0 = 0; k0 < vtot; k0 += 32)
+        // stage the chunk (coalesced: corner g * 32 + lane)
+        bool any = false;
+#pragma unroll
+        for (int g = 0; g < kExportPer; ++g)
         {
-            const int k = k0 + lane;
-            const int s = item_slot(vexcl, k);
-            const int es = __shfl_sync(0xffffffffu, vexcl, s);
-            const uint32_t bs = __shfl_sync(0xffffffffu, bits, s);
-            const int64_t ids = __shfl_sync(0xffffffffu, id, s);
-            const float v1s = __shfl_sync(0xffffffffu, v1, s);
-            if (k < vtot)
+            const int c = g * 32 + lane;
+            const int64_t t = wb + c;
+            const bool valid = t < n;
+            const uint32_t code = valid ? p.codes[t] : 0u;
+            const uint32_t em = valid ? p.emask[t] : 0u;
+            const int nv = __popc(em), nf = tab.count[code];
+            st.code[c] = static_cast<uint8_t>(code);
+            st.em[c] = static_cast<uint8_t>(em);
+            st.nv[c] = static_cast<uint8_t>(nv);
+            st.nf[c] = static_cast<uint8_t>(nf);
+            if (nv > 0 || nf > 0)
             {
-                const int a = nth_set_bit(bs, k - es);
+                st.id[c] = p.corners[t];
+                any = true;
+            }
+            if (nv > 0)
+                st.val[c] = p.values[t];
+        }
+        if (!__any_sync(0xffffffffu, any))
+            continue;
+        __syncwarp();
+        // prefix sums in corner order: lane l owns corners [4l, 4l + 4)
+        int vloc[kExportPer], floc[kExportPer];
+        int vt = 0, ft = 0;
+#pragma unroll
+        for (int g = 0; g < kExportPer; ++g)
+        {
+            const int c = lane * kExportPer + g;
+            vloc[g] = vt;
+            floc[g] = ft;
+            vt += st.nv[c];
+            ft += st.nf[c];
+        }
+        const int vin = warp_inclusive_scan(vt), fin = warp_inclusive_scan(ft);
+        const int vex = vin - vt, fex = fin - ft;
+        const int vtot = __shfl_sync(0xffffffffu, vin, 31), ftot = __shfl_sync(0xffffffffu, fin, 31);
+#pragma unroll
+        for (int g = 0; g < kExportPer; ++g)
+        {
+            st.vpre[lane * kExportPer + g] = vex + vloc[g];
+            st.fpre[lane * kExportPer + g] = fex + floc[g];
+        }
+        __syncwarp();
+
+        // vertices: the chunk's range starts at its first corner's vertex base
+        if (vtot > 0)
+        {
+            const int64_t vlo = p.vbase[wb];
+            for (int k = lane; k < vtot; k += 32)
+            {
+                const int c = stage_owner(st.vpre, k);
+                const int a = nth_set_bit(st.em[c], k - st.vpre[c]);
                 int64_t gx, gy, gz;
-                unpack_corner(ids, gx, gy, gz);
-                uint32_t r2 = static_cast<uint32_t>(wb + s + 1);
+                unpack_corner(st.id[c], gx, gy, gz);
+                uint32_t r2 = static_cast<uint32_t>(wb + c + 1);
                 if (a > 0)
                     corner_rank(p, gx, gy + (a == 1), gz + (a == 2), r2);
                 float v[3];
-                edge_vertex(p, gx, gy, gz, a, v1s, p.values[r2], scale, v);
+                edge_vertex(p, gx, gy, gz, a, st.val[c], p.values[r2], scale, v);
                 const int64_t out = vlo + k;
                 verts[3 * out + 0] = v[0];
                 verts[3 * out + 1] = v[1];
@@ -905,43 +962,28 @@ __global__ void __launch_bounds__(32 * kExportWarps) export_mesh_kernel(HullPlan
             }
         }
 
-        // faces
-        if (!__any_sync(0xffffffffu, cnt > 0))
-            continue;
-        const int64_t lo = __shfl_sync(0xffffffffu, valid ? static_cast<int64_t>(p.soup_off[t]) : int64_t{ 0 }, 0);
-        if (cnt > 0)
+        // faces: the chunk's entries are one contiguous range of the soup
+        // (soup_off is their exclusive prefix sum, a multiple of 3)
+        if (ftot > 0)
         {
-            int64_t gx, gy, gz;
-            unpack_corner(id, gx, gy, gz);
-            uint32_t rk[8];
-            cell_ranks(p, t, n, gx, gy, gz, rk);
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-                ranks[lane][i] = rk[i];
-        }
-        const int incl = warp_inclusive_scan(cnt);
-        const int excl = incl - cnt;
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        __syncwarp();
-        for (int k0 = 0; k0 < total; k0 += 32)
-        {
-            const int k = k0 + lane;
-            const int s = item_slot(excl, k);
-            const int es = __shfl_sync(0xffffffffu, excl, s);
-            const uint32_t cs = __shfl_sync(0xffffffffu, code, s);
-            if (k < total)
+            const int64_t lo = p.soup_off[wb];
+            for (int k = lane; k < ftot; k += 32)
             {
-                const uint32_t e = tab.edges[cs][k - es];
+                const int c = stage_owner(st.fpre, k);
+                const uint32_t e = tab.edges[st.code[c]][k - st.fpre[c]];
                 const int lo_corner = static_cast<int>(e & 7u), axis = static_cast<int>(e >> 3);
-                const int slot = k % 3; // lo is a multiple of 3
+                int64_t gx, gy, gz;
+                unpack_corner(st.id[c], gx, gy, gz);
+                // rank of the edge's lower corner (every corner of a cell with faces exists)
+                uint32_t r1 = static_cast<uint32_t>(wb + c);
+                if (lo_corner & 6)
+                    corner_rank(p, gx, gy + (lo_corner >> 1 & 1), gz + (lo_corner >> 2 & 1), r1);
+                r1 += static_cast<uint32_t>(lo_corner & 1);
+                const int slot = k % 3;
                 const int dst = k - slot + (slot == 0 ? 0 : 3 - slot);
-                const uint32_t r1 = ranks[s][lo_corner];
-                stage[dst] = static_cast<int64_t>(p.vbase[r1]) + __popc(p.emask[r1] & ((1u << axis) - 1u));
+                faces[lo + dst] = static_cast<int64_t>(p.vbase[r1]) + __popc(p.emask[r1] & ((1u << axis) - 1u));
             }
         }
-        __syncwarp();
-        for (int i = lane; i < total; i += 32)
-            faces[lo + i] = stage[i];
         __syncwarp();
     }
 }
