@@ -600,22 +600,34 @@ __device__ __forceinline__ bool cell_ranks(const HullPlan& p,
     if (!(gx < R - 1 && gy < R - 1 && gz < R - 1))
         return false;
     const int b = static_cast<int>(gx & 63);
+    // the four rows of corners (dy, dz) = (q & 1, q >> 1): their bitmap words
+    // and rank words are loaded together (independent loads), then checked
+    int64_t w[4];
+    uint64_t word[4], nextw[4];
+    uint32_t wrank[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q)
     {
-        // row of corners (dy, dz) = (q & 1, q >> 1); x + 1 < R stays in the row
-        const int64_t w = ((gy + (q & 1)) + (gz + (q >> 1)) * R) * p.WR + (gx >> 6);
-        const uint64_t word = p.bitmap[w];
-        const bool next = b < 63 ? ((word >> (b + 1)) & 1ull) != 0 : (p.bitmap[w + 1] & 1ull) != 0;
-        if (!next)
-            return false;
-        uint32_t r = static_cast<uint32_t>(t);
-        if (q > 0)
-        {
-            if (!((word >> b) & 1ull))
-                return false;
-            r = p.word_rank[w] + static_cast<uint32_t>(__popcll(word & ((1ull << b) - 1ull)));
-        }
+        w[q] = ((gy + (q & 1)) + (gz + (q >> 1)) * R) * p.WR + (gx >> 6);
+        word[q] = p.bitmap[w[q]];
+        wrank[q] = q > 0 ? p.word_rank[w[q]] : 0u;
+        // x + 1 < R stays in the row; at bit 63 the +x corner is bit 0 of the next word
+        nextw[q] = b == 63 ? p.bitmap[w[q] + 1] : 0ull;
+    }
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+    {
+        const bool next = b < 63 ? ((word[q] >> (b + 1)) & 1ull) != 0 : (nextw[q] & 1ull) != 0;
+        ok = ok && next && (q == 0 || ((word[q] >> b) & 1ull) != 0);
+    }
+    if (!ok)
+        return false;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+    {
+        const uint32_t r = q == 0 ? static_cast<uint32_t>(t)
+                                  : wrank[q] + static_cast<uint32_t>(__popcll(word[q] & ((1ull << b) - 1ull)));
         if (r + 1 >= n)
             return false;
         rk[2 * q] = r;
@@ -652,16 +664,22 @@ __global__ void __launch_bounds__(256) mc_cells_kernel(HullPlan p)
                 const uint32_t e = tab.edges[code][j];
                 used |= 1u << ((e & 7u) * 3u + (e >> 3));
             }
-            while (used)
+            // the vertex-edge bits of each lower corner, one word read and at
+            // most one atomic per corner (the reads are independent)
+            unsigned int* words[8];
+            uint32_t bits[8], cur[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
             {
-                const int k = __ffs(used) - 1;
-                used &= used - 1;
-                const uint32_t r1 = rk[k / 3];
-                const uint32_t bit = (1u << (k % 3)) << (8u * (r1 & 3u));
-                unsigned int* word = reinterpret_cast<unsigned int*>(p.emask) + (r1 >> 2);
-                if ((*word & bit) != bit)
-                    atomicOr(word, bit);
+                const uint32_t r1 = rk[i];
+                bits[i] = ((used >> (3 * i)) & 7u) << (8u * (r1 & 3u));
+                words[i] = reinterpret_cast<unsigned int*>(p.emask) + (r1 >> 2);
+                cur[i] = bits[i] ? *words[i] : 0u;
             }
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if ((cur[i] & bits[i]) != bits[i])
+                    atomicOr(words[i], bits[i]);
         }
         p.codes[t] = static_cast<uint8_t>(code);
     }
