@@ -320,6 +320,34 @@ def e2e_plain_pipelined(th, reqs, steps: int, dev, world: int) -> tuple[float, i
     return Q * steps * world / e2e_s, h2d, d2h
 
 
+def copy_bandwidth(reqs, dev, reps: int = 3) -> dict:
+    """Pinned host <-> device copy bandwidth of one request's masks, measured alone with CUDA events
+    (best of reps).  The end-to-end legs move these bytes every hull, so their result depends on
+    this bandwidth, which varies on a shared machine; it is reported beside them."""
+    import torch
+
+    src = reqs[0].masks
+    host = torch.empty(src.shape, dtype=src.dtype, pin_memory=True)
+    dst = torch.empty_like(src)
+    nbytes = src.numel() * src.element_size()
+    out = {}
+    for name, fn in (("h2d", lambda: dst.copy_(host, non_blocking=True)),
+                     ("d2h", lambda: host.copy_(src, non_blocking=True))):
+        best = float("inf")
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        out[f"{name}_gbs"] = nbytes / (best / 1000.0) / 1e9
+    out["bytes"] = nbytes
+    return out
+
+
 def run_gb300(args) -> dict | None:
     import torch
     import torch.distributed as dist
@@ -374,6 +402,7 @@ def run_gb300(args) -> dict | None:
 
     # end to end through the plain drop-in, copies pipelined against the hulls
     e2e_steps = args.steps
+    copy_gbs = copy_bandwidth(reqs, dev)
     e2e_value, h2d, d2h = e2e_plain_pipelined(th, reqs, e2e_steps, dev, world)
 
     # end to end through the batched form: while step k's batch runs, one side
@@ -488,7 +517,8 @@ def run_gb300(args) -> dict | None:
         "e2e": {"value": e2e_value, "unit": "hulls/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "path": "torchhull_gb300.visual_hull from pinned host memory; on one side stream the "
-                        "previous mesh out, then the next request in, overlapping the hull"},
+                        "previous mesh out, then the next request in, overlapping the hull",
+                "copy_bandwidth": copy_gbs},
         "e2e_batched": {"value": e2e_batched, "unit": "hulls/s",
                         "path": "th_visual_hull_batch per step; on one side stream the previous step's meshes out, "
                                 "then the next step's inputs in, overlapping the batch"},

@@ -68,6 +68,16 @@ __device__ __forceinline__ bool corner_rank(const HullPlan& p, int64_t x, int64_
     return true;
 }
 
+// Rank of a corner known to be set: the bitmap word and its rank word are
+// loaded together (no check of the bit in between).
+__device__ __forceinline__ uint32_t rank_of(const HullPlan& p, int64_t x, int64_t y, int64_t z)
+{
+    const int64_t w = (y + z * p.R) * p.WR + (x >> 6);
+    const uint64_t word = p.bitmap[w];
+    const uint32_t base = p.word_rank[w];
+    return base + static_cast<uint32_t>(__popcll(word & ((1ull << (x & 63)) - 1ull)));
+}
+
 __global__ void __launch_bounds__(256) mark_corners_kernel(HullPlan p)
 {
     const DevCounters* c = p.ctr;
@@ -958,25 +968,38 @@ __global__ void __launch_bounds__(32 * kExportWarps) export_mesh_kernel(HullPlan
         }
         __syncwarp();
 
-        // vertices: the chunk's range starts at its first corner's vertex base
+        // vertices: the chunk's range starts at its first corner's vertex base.
+        // Two entries per lane and iteration, their loads issued together;
+        // every corner looked up here exists, so the rank needs no check.
         if (vtot > 0)
         {
             const int64_t vlo = p.vbase[wb];
-            for (int k = lane; k < vtot; k += 32)
-            {
+            auto vertex_at = [&](int k, float v[3]) {
                 const int c = stage_owner(st.vpre, k);
                 const int a = nth_set_bit(st.em[c], k - st.vpre[c]);
                 int64_t gx, gy, gz;
                 unpack_corner(st.id[c], gx, gy, gz);
-                uint32_t r2 = static_cast<uint32_t>(wb + c + 1);
-                if (a > 0)
-                    corner_rank(p, gx, gy + (a == 1), gz + (a == 2), r2);
-                float v[3];
+                // the edge's upper corner (for a = 0 the next rank, wb + c + 1)
+                const uint32_t r2 = rank_of(p, gx + (a == 0), gy + (a == 1), gz + (a == 2));
                 edge_vertex(p, gx, gy, gz, a, st.val[c], p.values[r2], scale, v);
-                const int64_t out = vlo + k;
-                verts[3 * out + 0] = v[0];
-                verts[3 * out + 1] = v[1];
-                verts[3 * out + 2] = v[2];
+            };
+            for (int k = lane; k < vtot; k += 64)
+            {
+                const bool two = k + 32 < vtot;
+                float v0[3], v1[3];
+                vertex_at(k, v0);
+                vertex_at(two ? k + 32 : k, v1);
+                int64_t out = vlo + k;
+                verts[3 * out + 0] = v0[0];
+                verts[3 * out + 1] = v0[1];
+                verts[3 * out + 2] = v0[2];
+                if (two)
+                {
+                    out += 32;
+                    verts[3 * out + 0] = v1[0];
+                    verts[3 * out + 1] = v1[1];
+                    verts[3 * out + 2] = v1[2];
+                }
             }
         }
 
@@ -985,21 +1008,29 @@ __global__ void __launch_bounds__(32 * kExportWarps) export_mesh_kernel(HullPlan
         if (ftot > 0)
         {
             const int64_t lo = p.soup_off[wb];
-            for (int k = lane; k < ftot; k += 32)
-            {
+            auto face_at = [&](int k) -> int64_t {
                 const int c = stage_owner(st.fpre, k);
                 const uint32_t e = tab.edges[st.code[c]][k - st.fpre[c]];
                 const int lo_corner = static_cast<int>(e & 7u), axis = static_cast<int>(e >> 3);
                 int64_t gx, gy, gz;
                 unpack_corner(st.id[c], gx, gy, gz);
-                // rank of the edge's lower corner (every corner of a cell with faces exists)
-                uint32_t r1 = static_cast<uint32_t>(wb + c);
-                if (lo_corner & 6)
-                    corner_rank(p, gx, gy + (lo_corner >> 1 & 1), gz + (lo_corner >> 2 & 1), r1);
-                r1 += static_cast<uint32_t>(lo_corner & 1);
-                const int slot = k % 3;
-                const int dst = k - slot + (slot == 0 ? 0 : 3 - slot);
-                faces[lo + dst] = static_cast<int64_t>(p.vbase[r1]) + __popc(p.emask[r1] & ((1u << axis) - 1u));
+                // the edge's lower corner (every corner of a cell with faces exists)
+                const uint32_t r1 = rank_of(p, gx + (lo_corner & 1), gy + (lo_corner >> 1 & 1), gz + (lo_corner >> 2 & 1));
+                return static_cast<int64_t>(p.vbase[r1]) + __popc(p.emask[r1] & ((1u << axis) - 1u));
+            };
+            for (int k = lane; k < ftot; k += 64)
+            {
+                const bool two = k + 32 < ftot;
+                const int64_t f0 = face_at(k);
+                const int64_t f1 = face_at(two ? k + 32 : k);
+                // columns 1 and 2 swapped: entry k of a triangle goes to its mirror
+                const int s0 = k % 3;
+                faces[lo + k - s0 + (s0 == 0 ? 0 : 3 - s0)] = f0;
+                if (two)
+                {
+                    const int k1 = k + 32, s1 = k1 % 3;
+                    faces[lo + k1 - s1 + (s1 == 0 ? 0 : 3 - s1)] = f1;
+                }
             }
         }
         __syncwarp();
