@@ -105,3 +105,38 @@ def test_host_inputs_are_copied_in(th, cuda, requests):
     for r, (v, f) in zip(requests, got, strict=True):
         ev, ef = alone(th, r)
         assert v.is_cuda and torch.equal(v.cpu(), ev) and torch.equal(f.cpu(), ef)
+
+
+@pytest.mark.parametrize("large_bytes", [2e9, 2e8])
+@pytest.mark.parametrize("host", [False, True])
+def test_batched_serving_equals_results_alone(th, cuda, requests, host, large_bytes):
+    """max_batch > 1: requests pending together run as one batch on a slot's context; with the
+    smaller large_bytes some requests count as large, run alone and are skipped by the batches."""
+    from torchhull_gb300.serve import HullServer
+
+    reqs = requests + requests
+    if host:
+        reqs = [scenes.HullRequest(r.masks.cpu().pin_memory(), r.transforms.cpu(), r.level, r.cube_corner_bfl,
+                                   r.cube_length, r.masks_partial, r.transforms_convention) for r in reqs]
+    expected = [alone(th, r) for r in requests]
+    with HullServer(device=cuda.index or 0, slots=2, budget_bytes=20e9, max_batch=8,
+                    large_bytes=large_bytes) as server:
+        futures = [server.submit(r) for r in reqs]
+        got = [f.result(timeout=120) for f in futures]
+        stats = server.stats()
+    for k, (v, f) in enumerate(got):
+        ev, ef = expected[k % len(requests)]
+        assert torch.equal(v.cpu(), ev) and torch.equal(f.cpu(), ef), k
+    assert stats["completed"] == len(reqs)
+
+
+def test_batch_on_a_private_context(th, cuda, requests):
+    """HullContext.visual_hull_batch equals the plain drop-in on each request."""
+    ctx = th._C.HullContext(cuda.index or 0)
+    tuples = [(r.masks, r.transforms, r.level, r.cube_corner_bfl, r.cube_length, r.masks_partial,
+               r.transforms_convention, r.unique_verts) for r in requests]
+    for _ in range(2):
+        got = ctx.visual_hull_batch(tuples)
+        for r, (v, f) in zip(requests, got, strict=True):
+            ev, ef = alone(th, r)
+            assert torch.equal(v.cpu(), ev) and torch.equal(f.cpu(), ef)

@@ -489,7 +489,12 @@ int64_t launch_count()
 // cube_corner_bfl, cube_length, masks_partial, transforms_convention,
 // unique_verts), computed together on the device's context; returns the list
 // of (verts, faces).  All masks must be on one device.
-std::vector<std::tuple<at::Tensor, at::Tensor>> visual_hull_batch(const pybind11::list& requests)
+// Runs a batch on ctx (ctx == nullptr: the device's shared context, taken
+// under its lock); lock guards ctx otherwise.
+std::vector<std::tuple<at::Tensor, at::Tensor>> run_batch_on(const pybind11::list& requests,
+                                                             th_context* own_ctx,
+                                                             std::mutex* own_lock,
+                                                             int own_device)
 {
     const int64_t n = static_cast<int64_t>(requests.size());
     std::vector<std::tuple<at::Tensor, at::Tensor>> out;
@@ -519,16 +524,17 @@ std::vector<std::tuple<at::Tensor, at::Tensor>> visual_hull_batch(const pybind11
                                  t[4].cast<float>(), t[5].cast<bool>(), t[6].cast<std::string>(), t[7].cast<bool>()));
     }
     at::cuda::CUDAGuard guard(keep[0].device());
-    DeviceContext& dc = context_for(device);
-    auto g = lock_nogil(dc.lock);
+    TORCH_CHECK(!own_ctx || device == own_device, "masks are not on this context's device");
+    th_context* ctx = own_ctx ? own_ctx : context_for(device).ctx;
+    auto g = lock_nogil(own_lock ? *own_lock : context_for(device).lock);
     void* stream = stream_of(keep[0]);
     std::vector<th_hull_info> infos(n);
     th_status st;
     {
         pybind11::gil_scoped_release nogil;
-        st = th_visual_hull_batch(dc.ctx, args.data(), static_cast<int32_t>(n), stream, infos.data());
+        st = th_visual_hull_batch(ctx, args.data(), static_cast<int32_t>(n), stream, infos.data());
     }
-    check(st, dc.ctx);
+    check(st, ctx);
     const auto opts = at::TensorOptions().device(keep[0].device());
     std::vector<float*> vp(n);
     std::vector<int64_t*> fp(n);
@@ -540,8 +546,13 @@ std::vector<std::tuple<at::Tensor, at::Tensor>> visual_hull_batch(const pybind11
         fp[i] = f.data_ptr<int64_t>();
         out.emplace_back(v, f);
     }
-    check(th_visual_hull_batch_export_all(dc.ctx, static_cast<int32_t>(n), vp.data(), fp.data(), stream), dc.ctx);
+    check(th_visual_hull_batch_export_all(ctx, static_cast<int32_t>(n), vp.data(), fp.data(), stream), ctx);
     return out;
+}
+
+std::vector<std::tuple<at::Tensor, at::Tensor>> visual_hull_batch(const pybind11::list& requests)
+{
+    return run_batch_on(requests, nullptr, nullptr, -1);
 }
 
 // TH_OPTION_CARVE_KERNEL: 0 autotune, 1 views over lanes, 2 (parent, view) items.
@@ -639,6 +650,13 @@ public:
         return { verts, faces };
     }
 
+    // A batch of requests (the tuples of visual_hull_batch) on this context:
+    // one persistent carve launch over all of them, on the current stream.
+    std::vector<std::tuple<at::Tensor, at::Tensor>> visual_hull_batch(const pybind11::list& requests)
+    {
+        return run_batch_on(requests, ctx_, &lock_, device_);
+    }
+
     int64_t device_bytes() const
     {
         return th_context_device_bytes(ctx_);
@@ -704,5 +722,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
             .def(pybind11::init<int>(), "device"_a)
             .def("visual_hull", &HullContext::visual_hull, "masks"_a, "transforms"_a, "level"_a, "cube_corner_bfl"_a,
                  "cube_length"_a, "masks_partial"_a, "transforms_convention"_a, "unique_verts"_a = true)
+            .def("visual_hull_batch", &HullContext::visual_hull_batch, "requests"_a,
+                 "Batched visual hulls on this context: list of (masks, transforms, level, cube_corner_bfl, "
+                 "cube_length, masks_partial, transforms_convention, unique_verts) -> list of (verts, faces).")
             .def("device_bytes", &HullContext::device_bytes);
 }

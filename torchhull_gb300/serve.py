@@ -13,9 +13,12 @@ requests) and its own CUDA stream, so the kernels of concurrent requests
 overlap on the device.  A request is admitted when a slot
 is free and the device memory it needs fits in the admission budget together
 with the requests already running; otherwise it waits, and later requests
-that do fit may go first (no head-of-line blocking).  Every request's result
-is identical to running it alone: the kernels are deterministic and slots
-share no state.
+that do fit may go first (no head-of-line blocking).  With ``max_batch > 1`` a
+free slot takes all the pending requests that fit (up to that many) and runs
+them as one batch: one persistent carve launch over all their octrees, their
+integral images and mesh stages side by side on the slot's context.  Every
+request's result is identical to running it alone: the kernels are
+deterministic and slots share no state.
 
 The reference has no serving layer; this sits on top of the same C ABI as the
 drop-in ``visual_hull``.
@@ -64,7 +67,7 @@ def estimate_bytes(req: HullRequest) -> int:
     return int(inputs + sat + ones + cell_masks + node_pool + corner_pool + bitmap)
 
 
-@dataclasses.dataclass
+@dataclasses.dataclass(eq=False)  # jobs compare by identity (their requests hold tensors)
 class _Job:
     req: HullRequest
     future: concurrent.futures.Future
@@ -79,14 +82,22 @@ class HullServer:
     """Continuous-batching visual-hull server on one device."""
 
     def __init__(self, device: int = 0, slots: int = 4, budget_bytes: float = 60e9, priority: str = "none",
-                 large_bytes: float = 2e9):
+                 large_bytes: float = 2e9, max_batch: int = 1):
         """priority: how requests above large_bytes of estimated device memory (the ones that set
         the tail latency) share the GPU.  "exclusive_large": a large request waits until the
         running ones finish and then runs alone, and nothing is admitted while it waits or runs;
         "large_first" / "small_first": large / small requests run on high-priority CUDA streams,
-        so the block scheduler prefers their kernels; "none": all requests alike."""
+        so the block scheduler prefers their kernels; "none": all requests alike.
+
+        max_batch > 1: a slot that becomes free takes up to max_batch of the pending requests that
+        fit the budget together and runs them as one batch (th_visual_hull_batch: one persistent
+        carve launch over all of their octrees, their integral images and mesh stages side by
+        side); requests above large_bytes still run alone.  Results are the same either way."""
         if priority not in ("exclusive_large", "large_first", "small_first", "none"):
             raise ValueError(f"unknown priority policy {priority!r}")
+        if max_batch < 1:
+            raise ValueError("max_batch must be at least 1")
+        self.max_batch = int(max_batch)
         self.device = torch.device("cuda", device)
         self.budget = int(budget_bytes)
         self.priority = priority
@@ -160,7 +171,7 @@ class HullServer:
     def _is_large(self, job: _Job) -> bool:
         return job.bytes > self.large_bytes
 
-    def _admit(self) -> _Job | None:
+    def _admit_one(self) -> _Job | None:
         """First pending job that fits the budget (called with the lock held)."""
         exclusive = self.priority == "exclusive_large"
         if exclusive and self._large_running:
@@ -177,6 +188,27 @@ class HullServer:
                 return job
         return None
 
+    def _admit(self) -> list[_Job]:
+        """The jobs a free slot runs next (called with the lock held): the first pending job that
+        fits, and with batching the further small pending jobs that fit beside it."""
+        first = self._admit_one()
+        if first is None:
+            return []
+        jobs = [first]
+        if self.max_batch > 1 and not self._is_large(first):
+            need = first.bytes
+            keep: collections.deque[_Job] = collections.deque()
+            while self._pending:
+                job = self._pending.popleft()
+                if (len(jobs) < self.max_batch and not self._is_large(job)
+                        and self._running_bytes + need + job.bytes <= self.budget):
+                    jobs.append(job)
+                    need += job.bytes
+                else:
+                    keep.append(job)
+            self._pending = keep
+        return jobs
+
     def _stream_for(self, slot: int, job: _Job) -> torch.cuda.Stream:
         large = job.bytes > self.large_bytes
         hi = (self.priority == "large_first" and large) or (self.priority == "small_first" and not large)
@@ -186,42 +218,61 @@ class HullServer:
         ctx = self._contexts[slot]
         while True:
             with self._cv:
-                job = None
-                while job is None:
-                    job = self._admit()
-                    if job is None:
-                        if self._closed and not self._pending:
-                            return
-                        self._cv.wait()
-                self._in_flight += 1
-                self._running_bytes += job.bytes
-            job.started = time.perf_counter()
-            stream = self._stream_for(slot, job)
+                jobs: list[_Job] = []
+                try:
+                    while not jobs:
+                        jobs = self._admit()
+                        if not jobs:
+                            if self._closed and not self._pending:
+                                return
+                            self._cv.wait()
+                except Exception as exc:  # a broken scheduler must not leave callers waiting
+                    for job in list(self._pending) + jobs:
+                        if not job.future.done():
+                            job.future.set_exception(exc)
+                    self._pending.clear()
+                    self._closed = True
+                    self._cv.notify_all()
+                    return
+                self._in_flight += len(jobs)
+                self._running_bytes += sum(job.bytes for job in jobs)
+            started = time.perf_counter()
+            for job in jobs:
+                job.started = started
+            stream = self._stream_for(slot, jobs[0])
             try:
-                r = job.req
                 with torch.cuda.stream(stream):
-                    if job.ready is not None:
-                        stream.wait_event(job.ready)
-                    masks = r.masks.to(self.device, non_blocking=True)
-                    transforms = r.transforms.to(self.device, non_blocking=True)
-                    verts, faces = ctx.visual_hull(masks, transforms, r.level, r.cube_corner_bfl, r.cube_length,
-                                                   r.masks_partial, r.transforms_convention, r.unique_verts)
-                    if job.consumer != stream:
-                        verts.record_stream(job.consumer)
-                        faces.record_stream(job.consumer)
+                    args = []
+                    for job in jobs:
+                        r = job.req
+                        if job.ready is not None:
+                            stream.wait_event(job.ready)
+                        masks = r.masks.to(self.device, non_blocking=True)
+                        transforms = r.transforms.to(self.device, non_blocking=True)
+                        args.append((masks, transforms, r.level, r.cube_corner_bfl, r.cube_length, r.masks_partial,
+                                     r.transforms_convention, r.unique_verts))
+                    outs = [ctx.visual_hull(*args[0])] if len(jobs) == 1 else ctx.visual_hull_batch(args)
+                    for job, (verts, faces) in zip(jobs, outs, strict=True):
+                        if job.consumer != stream:
+                            verts.record_stream(job.consumer)
+                            faces.record_stream(job.consumer)
                 stream.synchronize()
                 done = time.perf_counter()
-                job.future.set_result((verts, faces))
+                for job, out in zip(jobs, outs, strict=True):
+                    job.future.set_result(tuple(out))
                 with self._cv:
-                    self.latencies_ms.append(1000.0 * (done - job.arrival))
-                    self.queue_ms.append(1000.0 * (job.started - job.arrival))
-                    self.completed += 1
-            except Exception as exc:  # surfaced to the caller through the future
-                job.future.set_exception(exc)
+                    for job in jobs:
+                        self.latencies_ms.append(1000.0 * (done - job.arrival))
+                        self.queue_ms.append(1000.0 * (job.started - job.arrival))
+                    self.completed += len(jobs)
+            except Exception as exc:  # surfaced to the callers through the futures
+                for job in jobs:
+                    if not job.future.done():
+                        job.future.set_exception(exc)
             finally:
                 with self._cv:
-                    self._in_flight -= 1
-                    self._running_bytes -= job.bytes
-                    if self.priority == "exclusive_large" and self._is_large(job):
+                    self._in_flight -= len(jobs)
+                    self._running_bytes -= sum(job.bytes for job in jobs)
+                    if self.priority == "exclusive_large" and any(self._is_large(job) for job in jobs):
                         self._large_running = False
                     self._cv.notify_all()
