@@ -718,8 +718,8 @@ def serve_measure(args, th, scenes, dev, world, rank, policies=("none", "large_f
         """burst > 0: that many requests from the pool submitted at once (capacity), else the arrivals."""
         with HullServer(device=dev.index or 0, slots=slots, budget_bytes=60e9, priority=priority,
                         max_batch=max_batch) as server:
-            for r in pool[:slots] + large[:1]:  # each slot's context allocates its pools once
-                server.submit(r).result(timeout=600)
+            # every slot's context: pools sized, carve kernel tuned, graphs captured for the pool's shapes
+            server.warm_up(pool + large[:1])
             server.latencies_ms.clear()
             server.queue_ms.clear()
             t0 = time.perf_counter()

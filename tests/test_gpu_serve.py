@@ -140,3 +140,14 @@ def test_batch_on_a_private_context(th, cuda, requests):
         for r, (v, f) in zip(requests, got, strict=True):
             ev, ef = alone(th, r)
             assert torch.equal(v.cpu(), ev) and torch.equal(f.cpu(), ef)
+
+
+def test_warm_up_then_serve(th, cuda, requests):
+    from torchhull_gb300.serve import HullServer
+
+    with HullServer(device=cuda.index or 0, slots=2, max_batch=4) as server:
+        server.warm_up(requests[:3])
+        got = [f.result(timeout=120) for f in [server.submit(r) for r in requests[:3]]]
+    for r, (v, f) in zip(requests[:3], got, strict=True):
+        ev, ef = alone(th, r)
+        assert torch.equal(v.cpu(), ev) and torch.equal(f.cpu(), ef)

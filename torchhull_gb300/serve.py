@@ -142,6 +142,25 @@ class HullServer:
             self._cv.notify_all()
         return fut
 
+    def warm_up(self, requests: list[HullRequest]) -> None:
+        """Runs every request once on every slot's context (and, with batching, in batches of
+        max_batch), synchronously: each context then has its pools sized, its carve kernel tuned
+        and its CUDA graphs captured for these request shapes before timed traffic arrives.
+        Call it before submitting requests."""
+        for slot, ctx in enumerate(self._contexts):
+            stream = self._streams[slot]
+            with torch.cuda.stream(stream):
+                args = [(r.masks.to(self.device, non_blocking=True), r.transforms.to(self.device, non_blocking=True),
+                         r.level, r.cube_corner_bfl, r.cube_length, r.masks_partial, r.transforms_convention,
+                         r.unique_verts) for r in requests]
+                for a in args:
+                    ctx.visual_hull(*a)
+                if self.max_batch > 1:
+                    small = [a for a, r in zip(args, requests, strict=True) if estimate_bytes(r) <= self.large_bytes]
+                    for i in range(0, len(small), self.max_batch):
+                        ctx.visual_hull_batch(small[i:i + self.max_batch])
+            stream.synchronize()
+
     def close(self) -> None:
         with self._cv:
             self._closed = True
