@@ -181,6 +181,16 @@ def percentile(sorted_vals: list[float], p: float) -> float | None:
     return sorted_vals[min(len(sorted_vals) - 1, int(round(p / 100.0 * (len(sorted_vals) - 1))))]
 
 
+def replica_seeds(rank: int, count: int, base: int = 3) -> list[int]:
+    """Seeds of a rank's own requests: every rank serves different scenes (replicas, weak scaling)."""
+    return [base + 1000 * rank + q for q in range(count)]
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds_max: float) -> float:
+    """Units of all ranks per second of the slowest rank (the job ends when the last rank does)."""
+    return units_per_rank * world / seconds_max
+
+
 def max_over_ranks(x: float, world: int, dev) -> float:
     import torch
     import torch.distributed as dist
@@ -375,7 +385,7 @@ def run_gb300(args) -> dict | None:
         return finish(run_blur(args, th, scenes, dev, world, rank), world)
 
     Q = args.requests
-    reqs = [scenes.partial_request(device=dev, seed=3 + 1000 * rank + q) for q in range(Q)]
+    reqs = [scenes.partial_request(device=dev, seed=seed) for seed in replica_seeds(rank, Q)]
     tuples = [as_tuple(r) for r in reqs]
     torch.cuda.synchronize()
     for _ in range(args.warmup):
@@ -391,7 +401,7 @@ def run_gb300(args) -> dict | None:
     batch_ms = timed_batches(th, tuples, args.steps, dev, world)
     clocks = sampler.stop()
     launches = th._C.launch_count() - launches0
-    value = Q * args.steps * world / (batch_ms / 1000.0)
+    value = whole_job_rate(Q * args.steps, world, batch_ms / 1000.0)
 
     # plain drop-in: throughput and latency as a caller sees them (stage events
     # off, so the pipeline is replayed as a CUDA graph), then stage times from
