@@ -67,6 +67,12 @@ from pathlib import Path
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
+# CUDA maps streams onto a few hardware work queues (8 by default), and streams
+# that share one can wait on each other's work.  This process runs the
+# library's own streams, the serving slots' and the copy stream of the
+# end-to-end legs beside the hulls' stream: give them 32 queues.  Must be set
+# before CUDA initialises.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 LEVEL = 9
 VIEWS = 32
@@ -257,21 +263,37 @@ def timed_plain(th, reqs, steps: int, dev, world: int, local: int, profile: bool
     return max_over_ranks(start.elapsed_time(stop), world, dev), sorted(per_hull), stages
 
 
-def e2e_plain_pipelined(th, reqs, steps: int, dev, world: int) -> tuple[float, int, int]:
+def host_copy(th, method: str):
+    """The copy the end-to-end legs move their bytes with, on the current stream: "sm" is
+    torchhull_gb300's copy kernel (th_copy: a few blocks of SMs over the pinned buffers' device
+    mappings), "dma" is cudaMemcpyAsync (a copy engine).  With copy-engine copies overlapping the
+    hulls, about one loop of three on GB300 lost ~70-80 ms to a stall (either direction alone
+    was enough); the copy kernel showed none in 40 loops and ran ~5% below the stall-free loops."""
+    if method == "sm":
+        return th._C.copy_on_sms
+
+    def dma(dst, src):
+        dst.copy_(src, non_blocking=True)
+
+    return dma
+
+
+def e2e_plain_pipelined(th, reqs, steps: int, dev, world: int, copy: str = "sm") -> tuple[float, int, int, dict]:
     """End to end through the plain drop-in (torchhull_gb300.visual_hull) from
     pinned host memory: hull i runs on the compute stream while one copy stream
     first copies hull i-1's mesh out to pinned host memory and then request
     i+1's masks and transforms in (two device slots).  Every copy of every step
-    is inside the timed region.  Returns (hulls/s, h2d bytes per step, d2h bytes
-    per step).
+    is inside the timed region; copy names the copy method (host_copy).
+    Returns (hulls/s, h2d bytes per step, d2h bytes per step, allocator
+    counters of the timed loop).
 
-    The two directions share one stream on purpose: run at the same time on two
-    streams, the copy-in and the copy-out slowed the hull they overlap by ~0.7 ms
-    on GB300 (216-231 against 279 hulls/s, with 286 for the same loop without
-    copies)."""
+    The two directions share one stream, so one copy at a time runs beside a
+    hull (per hull 134 MB in at ~130 GB/s and ~211 MB out at ~190 GB/s with
+    the copy kernel: ~2.2 ms, inside the ~3.1 ms hull)."""
     import torch
     import torch.distributed as dist
 
+    xfer = host_copy(th, copy)
     Q = len(reqs)
     shape, tshape = reqs[0].masks.shape, reqs[0].transforms.shape
     assert all(r.masks.shape == shape and r.transforms.shape == tshape for r in reqs)
@@ -292,42 +314,52 @@ def e2e_plain_pipelined(th, reqs, steps: int, dev, world: int) -> tuple[float, i
     free = [torch.cuda.Event() for _ in range(2)]
     order = [q for _ in range(steps) for q in range(Q)]
 
-    def copy_in(i):
+    def copy_in(order, i):
         s = i % 2
         with torch.cuda.stream(copies):
             copies.wait_event(free[s])  # hull i-2 is done with slot s
-            slots[s][0].copy_(host_in[order[i]][0], non_blocking=True)
-            slots[s][1].copy_(host_in[order[i]][1], non_blocking=True)
+            xfer(slots[s][0], host_in[order[i]][0])
+            xfer(slots[s][1], host_in[order[i]][1])
             ready[s].record(copies)
 
+    def run(order):
+        for i in range(min(2, len(order))):
+            copy_in(order, i)
+        for i, q in enumerate(order):
+            s = i % 2
+            comp.wait_event(ready[s])
+            kw = reqs[q].kwargs()
+            kw["masks"], kw["transforms"] = slots[s]
+            v, f = th.visual_hull(**kw)
+            free[s].record(comp)
+            done = torch.cuda.Event()
+            done.record(comp)
+            # on the copy stream: hull i's mesh out, then request i+2's inputs in
+            # (into the slot hull i has just released); both overlap hull i+1
+            with torch.cuda.stream(copies):
+                copies.wait_event(done)
+                xfer(host_out[q][0], v)
+                xfer(host_out[q][1], f)
+                v.record_stream(copies)
+                f.record_stream(copies)
+            if i + 2 < len(order):
+                copy_in(order, i + 2)
+        torch.cuda.synchronize()
+
+    # one untimed pass of the same loop: the caching allocator settles on the
+    # blocks this pattern of allocations and cross-stream frees needs
+    run(list(range(Q)))
+    stats0 = torch.cuda.memory_stats(dev)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for i in range(min(2, len(order))):
-        copy_in(i)
-    for i, q in enumerate(order):
-        s = i % 2
-        comp.wait_event(ready[s])
-        kw = reqs[q].kwargs()
-        kw["masks"], kw["transforms"] = slots[s]
-        v, f = th.visual_hull(**kw)
-        free[s].record(comp)
-        done = torch.cuda.Event()
-        done.record(comp)
-        # on the copy stream: hull i's mesh out, then request i+2's inputs in
-        # (into the slot hull i has just released); both overlap hull i+1
-        with torch.cuda.stream(copies):
-            copies.wait_event(done)
-            host_out[q][0].copy_(v, non_blocking=True)
-            host_out[q][1].copy_(f, non_blocking=True)
-            v.record_stream(copies)
-            f.record_stream(copies)
-        if i + 2 < len(order):
-            copy_in(i + 2)
-    torch.cuda.synchronize()
+    run(order)
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
-    return Q * steps * world / e2e_s, h2d, d2h
+    stats1 = torch.cuda.memory_stats(dev)
+    allocator = {k: stats1.get(k, 0) - stats0.get(k, 0)
+                 for k in ("segment.all.allocated", "segment.all.freed", "num_alloc_retries")}
+    return Q * steps * world / e2e_s, h2d, d2h, allocator
 
 
 def copy_bandwidth(reqs, dev, reps: int = 3) -> dict:
@@ -413,7 +445,10 @@ def run_gb300(args) -> dict | None:
     # end to end through the plain drop-in, copies pipelined against the hulls
     e2e_steps = args.steps
     copy_gbs = copy_bandwidth(reqs, dev)
-    e2e_value, h2d, d2h = e2e_plain_pipelined(th, reqs, e2e_steps, dev, world)
+    e2e_value, h2d, d2h, e2e_alloc = e2e_plain_pipelined(th, reqs, e2e_steps, dev, world, copy=args.e2e_copy)
+    # the same loop once with the other copy method, for comparison
+    other_copy = "dma" if args.e2e_copy == "sm" else "sm"
+    e2e_other = e2e_plain_pipelined(th, reqs, e2e_steps, dev, world, copy=other_copy)[0]
 
     # end to end through the batched form: while step k's batch runs, one side
     # stream copies step k-1's meshes out and then step k+1's inputs in (two
@@ -428,41 +463,50 @@ def run_gb300(args) -> dict | None:
     copies = torch.cuda.Stream(dev)
     ready = [torch.cuda.Event() for _ in range(2)]
     free = [torch.cuda.Event() for _ in range(2)]
+    xfer = host_copy(th, args.e2e_copy)
 
     def batch_in(k):
         s = k % 2
         with torch.cuda.stream(copies):
             copies.wait_event(free[s])  # step k-2 is done with slot s
             for q in range(Q):
-                slots[s][q][0].copy_(host_masks[q], non_blocking=True)
-                slots[s][q][1].copy_(host_tf[q], non_blocking=True)
+                xfer(slots[s][q][0], host_masks[q])
+                xfer(slots[s][q][1], host_tf[q])
             ready[s].record(copies)
 
+    def run_batches(steps):
+        for k in range(min(2, steps)):
+            batch_in(k)
+        for k in range(steps):
+            s = k % 2
+            comp.wait_event(ready[s])
+            out = th._C.visual_hull_batch([slots[s][q] + tuples[q][2:] for q in range(Q)])
+            free[s].record(comp)
+            done = torch.cuda.Event()
+            done.record(comp)
+            with torch.cuda.stream(copies):
+                copies.wait_event(done)
+                for (v, f), (vh, fh) in zip(out, host_out, strict=True):
+                    xfer(vh, v)
+                    xfer(fh, f)
+                    v.record_stream(copies)
+                    f.record_stream(copies)
+            if k + 2 < steps:
+                batch_in(k + 2)
+        torch.cuda.synchronize()
+
+    run_batches(2)  # untimed: the allocator settles on this loop's blocks
+    bstats0 = torch.cuda.memory_stats(dev)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for k in range(min(2, e2e_steps)):
-        batch_in(k)
-    for k in range(e2e_steps):
-        s = k % 2
-        comp.wait_event(ready[s])
-        out = th._C.visual_hull_batch([slots[s][q] + tuples[q][2:] for q in range(Q)])
-        free[s].record(comp)
-        done = torch.cuda.Event()
-        done.record(comp)
-        with torch.cuda.stream(copies):
-            copies.wait_event(done)
-            for (v, f), (vh, fh) in zip(out, host_out, strict=True):
-                vh.copy_(v, non_blocking=True)
-                fh.copy_(f, non_blocking=True)
-                v.record_stream(copies)
-                f.record_stream(copies)
-        if k + 2 < e2e_steps:
-            batch_in(k + 2)
-    torch.cuda.synchronize()
+    run_batches(e2e_steps)
     e2e_batched = Q * e2e_steps * world / max_over_ranks(time.perf_counter() - t0, world, dev)
-    del slots, host_out, out, first
+    bstats1 = torch.cuda.memory_stats(dev)
+    e2e_batched_alloc = {k: bstats1.get(k, 0) - bstats0.get(k, 0)
+                         for k in ("segment.all.allocated", "segment.all.freed", "num_alloc_retries")}
+    del slots, host_out, first
 
     # the other configurations and the reference's CUDA build, measured after the timed region
     # (one GPU only: under torchrun every rank times the headline alone)
@@ -528,10 +572,12 @@ def run_gb300(args) -> dict | None:
                 "d2h_bytes_per_step": d2h,
                 "path": "torchhull_gb300.visual_hull from pinned host memory; on one side stream the "
                         "previous mesh out, then the next request in, overlapping the hull",
-                "copy_bandwidth": copy_gbs},
+                "copy_method": args.e2e_copy, f"value_with_{other_copy}_copies": e2e_other,
+                "copy_bandwidth": copy_gbs, "allocator_in_timed_loop": e2e_alloc},
         "e2e_batched": {"value": e2e_batched, "unit": "hulls/s",
                         "path": "th_visual_hull_batch per step; on one side stream the previous step's meshes out, "
-                                "then the next step's inputs in, overlapping the batch"},
+                                "then the next step's inputs in, overlapping the batch",
+                        "allocator_in_timed_loop": e2e_batched_alloc},
         "roofline": {"bound": "hbm", "kernel": dom[1], "stage": dom[0], "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes": dom[3], "ms": dom[2], "traffic": NCU_TRAFFIC.get(dom[0]),
@@ -976,6 +1022,8 @@ def main() -> None:
     ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--no-hetero", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--e2e-copy", choices=["dma", "sm"], default="sm",
+                    help="end-to-end legs: host <-> device copies by copy engines or by the copy kernel")
     ap.add_argument("--batch-route", choices=["on", "off"], default="off",
                     help="batched form: requests that fill the GPU alone through the per-request pipeline")
     ap.add_argument("--field-ones", choices=["on", "off"], default="on",

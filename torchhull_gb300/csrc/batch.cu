@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(256) batch_cell_masks_kernel(BatchPlan bp, boo
 
 void launch_batch_init(const BatchPlan& bp, cudaStream_t s)
 {
-    TH_CUDA(cudaMemsetAsync(bp.ctr, 0, sizeof(BatchCounters), s));
+    launch_zero(bp.ctr, sizeof(BatchCounters), s);
     batch_init_kernel<<<1, 256, 0, s>>>(bp);
     TH_LAUNCH_CHECK();
 }

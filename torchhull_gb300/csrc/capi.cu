@@ -71,6 +71,65 @@ int sm_count()
 namespace
 {
 
+// Small host <-> device transfers (request constants in, counters out) run
+// as a one-block kernel over mapped pinned host memory instead of
+// cudaMemcpyAsync: a copy engine may be busy with a caller's bulk copy on
+// another stream (a previous mesh going out, the next request's masks coming
+// in), and a small copy queued behind it would stall the whole pipeline.
+__global__ void small_copy_kernel(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst, int64_t n)
+{
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+        dst[i] = src[i];
+    __threadfence_system();
+}
+
+__global__ void zero_kernel(unsigned char* __restrict__ p, int64_t n)
+{
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+        p[i] = 0;
+}
+
+// dst and src are device addresses (device memory, or mapped host memory's device address).
+void small_copy(void* dst, const void* src, size_t bytes, cudaStream_t st)
+{
+    small_copy_kernel<<<1, 256, 0, st>>>(static_cast<const unsigned char*>(src), static_cast<unsigned char*>(dst),
+                                          static_cast<int64_t>(bytes));
+    TH_LAUNCH_CHECK();
+}
+
+// Pinned host memory for count objects of T, mapped into the device's address space.
+template <typename T>
+void alloc_mapped(T** host, T** dev, size_t count = 1)
+{
+    void* h = nullptr;
+    TH_CUDA(cudaHostAlloc(&h, sizeof(T) * count, cudaHostAllocMapped));
+    void* d = nullptr;
+    const cudaError_t e = cudaHostGetDevicePointer(&d, h, 0);
+    if (e != cudaSuccess)
+    {
+        cudaFreeHost(h);
+        throw CudaError{ e, "cudaHostGetDevicePointer" };
+    }
+    *host = static_cast<T*>(h);
+    *dev = static_cast<T*>(d);
+}
+
+}  // namespace
+
+void launch_zero(void* p, size_t bytes, cudaStream_t s)
+{
+    if (bytes == 0)
+        return;
+    const int64_t n = static_cast<int64_t>(bytes);
+    const unsigned grid = static_cast<unsigned>(std::min<int64_t>((n + 255) / 256, 64));
+    zero_kernel<<<grid, 256, 0, s>>>(static_cast<unsigned char*>(p), n);
+    TH_LAUNCH_CHECK();
+}
+
+namespace
+{
+
 struct DevBuf
 {
     void* p = nullptr;
@@ -128,9 +187,11 @@ struct HullSlot
             word_rank, rowbits, rows, corners, values, codes, emask, soup_off, vbase, counters, flags, sat_scratch;
     int64_t node_cap = 0, corner_cap = 0, parent_cap = 0;
     HullPlan plan{};
-    DevCounters* host = nullptr; // pinned copy of the counters
+    DevCounters* host = nullptr; // pinned, mapped copy of the counters
+    DevCounters* host_d = nullptr; // its device address
     DevBuf rq;                   // ReqConsts of the running request (device)
-    ReqConsts* host_rq = nullptr; // pinned source of rq
+    ReqConsts* host_rq = nullptr; // pinned, mapped source of rq
+    ReqConsts* host_rq_d = nullptr; // its device address
     th_hull_info info{};
     bool has_result = false;
     bool dirty = false; // bitmap rows of the last request still set
@@ -169,9 +230,11 @@ struct HullSlot
         if (host)
             cudaFreeHost(host);
         host = nullptr;
+        host_d = nullptr;
         if (host_rq)
             cudaFreeHost(host_rq);
         host_rq = nullptr;
+        host_rq_d = nullptr;
         if (capture_stream)
             cudaStreamDestroy(capture_stream);
         capture_stream = nullptr;
@@ -269,9 +332,11 @@ namespace
 struct BatchState
 {
     DevBuf reqs, nodes, node_skip, node_out, ctr, child_masks, child_skip, child_out, block_sums;
-    BatchReq* host_reqs = nullptr; // pinned
+    BatchReq* host_reqs = nullptr; // pinned, mapped
+    BatchReq* host_reqs_d = nullptr; // its device address
     int32_t host_reqs_cap = 0;
-    BatchCounters* host_ctr = nullptr; // pinned
+    BatchCounters* host_ctr = nullptr; // pinned, mapped
+    BatchCounters* host_ctr_d = nullptr; // its device address
     int64_t node_cap = 0;
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> joins;
@@ -287,6 +352,8 @@ struct BatchState
             cudaFreeHost(host_ctr);
         host_reqs = nullptr;
         host_ctr = nullptr;
+        host_reqs_d = nullptr;
+        host_ctr_d = nullptr;
         for (auto s : streams)
             cudaStreamDestroy(s);
         for (auto e : joins)
@@ -311,7 +378,8 @@ namespace
 struct McSlot
 {
     DevBuf groups, keys, slots, codes, used, vbase, tiles_soup, tiles_verts, tiles_scan, active, active_soup, ctr;
-    McCounters* host = nullptr; // pinned copy of the counters
+    McCounters* host = nullptr; // pinned, mapped copy of the counters
+    McCounters* host_d = nullptr; // its device address
     McPlan plan{};
     th_mc_info info{};
     bool has_result = false;
@@ -494,7 +562,7 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_one
     if (s.counters.ensure(sizeof(DevCounters)))
         TH_CUDA(cudaMemsetAsync(s.counters.p, 0, sizeof(DevCounters), st));
     if (!s.host)
-        TH_CUDA(cudaMallocHost(&s.host, sizeof(DevCounters)));
+        alloc_mapped(&s.host, &s.host_d);
     if (!s.done)
         TH_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
 
@@ -555,9 +623,9 @@ void prepare(HullSlot& s, const th_hull_args* a, cudaStream_t st, bool field_one
     // the per-request inputs the carve and field kernels read from the device
     s.rq.ensure(sizeof(ReqConsts));
     if (!s.host_rq)
-        TH_CUDA(cudaMallocHost(&s.host_rq, sizeof(ReqConsts)));
+        alloc_mapped(&s.host_rq, &s.host_rq_d);
     *s.host_rq = ReqConsts{ { p.corner[0], p.corner[1], p.corner[2] }, p.length, p.masks };
-    TH_CUDA(cudaMemcpyAsync(s.rq.p, s.host_rq, sizeof(ReqConsts), cudaMemcpyHostToDevice, st));
+    small_copy(s.rq.p, s.host_rq_d, sizeof(ReqConsts), st);
     p.rq = s.rq.as<ReqConsts>();
 }
 
@@ -626,7 +694,7 @@ void enqueue_core(th_context* ctx, HullSlot& s, cudaStream_t st, StageEvents* ev
     launch_marching_cubes(p, st);
     if (ev)
         ev->record(L + 5, st);
-    TH_CUDA(cudaMemcpyAsync(s.host, p.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+    small_copy(s.host_d, p.ctr, sizeof(DevCounters), st);
 }
 
 // enqueue_core as a graph: captured once per plan (the per-request corner,
@@ -709,7 +777,7 @@ void run_hull_once(th_context* ctx,
             if (ev)
                 ev->record(0, st);
             launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), st);
-            TH_CUDA(cudaMemsetAsync(s.flags.p, 0, sizeof(unsigned int), st));
+            launch_zero(s.flags.p, sizeof(unsigned int), st);
             launch_integral_image(a->masks, a->masks_dtype, a->batch, a->height, a->width, s.sat.as<float>(), st,
                                   s.flags.as<unsigned int>(),
                                   ctx->sat_single_pass ? SatScratch{ s.sat_scratch.p } : SatScratch{});
@@ -827,11 +895,11 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
     {
         if (bs.host_reqs)
             TH_CUDA(cudaFreeHost(bs.host_reqs));
-        TH_CUDA(cudaMallocHost(&bs.host_reqs, sizeof(BatchReq) * n));
+        alloc_mapped(&bs.host_reqs, &bs.host_reqs_d, n);
         bs.host_reqs_cap = n;
     }
     if (!bs.host_ctr)
-        TH_CUDA(cudaMallocHost(&bs.host_ctr, sizeof(BatchCounters)));
+        alloc_mapped(&bs.host_ctr, &bs.host_ctr_d);
     int max_level = 0;
     int64_t want_nodes = 0;
     for (int32_t r = 0; r < n; ++r)
@@ -872,7 +940,7 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
             const th_hull_args* a = &args[r];
             HullSlot& s = ctx->batch[r];
             prepare(s, a, st, ctx->field_ones, ctx->field_masks, true);
-            TH_CUDA(cudaMemsetAsync(s.plan.ctr, 0, sizeof(DevCounters), st));
+            launch_zero(s.plan.ctr, sizeof(DevCounters), st);
             const HullPlan& p = s.plan;
             BatchReq& q = bs.host_reqs[r];
             q = BatchReq{};
@@ -911,7 +979,7 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
                 HullSlot& s = ctx->batch[r];
                 cudaStream_t sr = bs.streams[r % nstreams];
                 launch_convert_transforms(a->transforms, a->transforms_dtype, a->batch, s.tf.as<float>(), sr);
-                TH_CUDA(cudaMemsetAsync(s.flags.p, 0, sizeof(unsigned int), sr));
+                launch_zero(s.flags.p, sizeof(unsigned int), sr);
                 launch_integral_image(a->masks, a->masks_dtype, a->batch, a->height, a->width, s.sat.as<float>(), sr,
                                       s.flags.as<unsigned int>(),
                                       ctx->sat_single_pass ? SatScratch{ s.sat_scratch.p } : SatScratch{});
@@ -922,7 +990,7 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
                 TH_CUDA(cudaStreamWaitEvent(st, bs.joins[i], 0));
             }
         }
-        TH_CUDA(cudaMemcpyAsync(bs.reqs.p, bs.host_reqs, sizeof(BatchReq) * n, cudaMemcpyHostToDevice, st));
+        small_copy(bs.reqs.p, bs.host_reqs_d, sizeof(BatchReq) * n, st);
         BatchPlan bp{};
         bp.reqs = bs.reqs.as<BatchReq>();
         bp.nreq = n;
@@ -977,10 +1045,9 @@ void run_batch(th_context* ctx, const th_hull_args* args, int32_t n, cudaStream_
             TH_CUDA(cudaStreamWaitEvent(st, bs.joins[i], 0));
         }
         launch_batch_cell_masks(bp, false, st);
-        TH_CUDA(cudaMemcpyAsync(bs.host_ctr, bp.ctr, sizeof(BatchCounters), cudaMemcpyDeviceToHost, st));
+        small_copy(bs.host_ctr_d, bp.ctr, sizeof(BatchCounters), st);
         for (int32_t r = 0; r < n; ++r)
-            TH_CUDA(cudaMemcpyAsync(ctx->batch[r].host, ctx->batch[r].plan.ctr, sizeof(DevCounters),
-                                    cudaMemcpyDeviceToHost, st));
+            small_copy(ctx->batch[r].host_d, ctx->batch[r].plan.ctr, sizeof(DevCounters), st);
         TH_CUDA(cudaStreamSynchronize(st));
         bool retry = false;
         if (bs.host_ctr->overflow)
@@ -1208,7 +1275,7 @@ void run_mc(McSlot& s, const th_mc_args* a, cudaStream_t st)
     }
 
     if (!s.host)
-        TH_CUDA(cudaMallocHost(&s.host, sizeof(McCounters)));
+        alloc_mapped(&s.host, &s.host_d);
     s.ctr.ensure(sizeof(McCounters));
     p.ctr = s.ctr.as<McCounters>();
     if (p.sparse)
@@ -1254,7 +1321,7 @@ void run_mc(McSlot& s, const th_mc_args* a, cudaStream_t st)
     }
 
     launch_mc_count(p, st);
-    TH_CUDA(cudaMemcpyAsync(s.host, p.ctr, sizeof(McCounters), cudaMemcpyDeviceToHost, st));
+    small_copy(s.host_d, p.ctr, sizeof(McCounters), st);
     TH_CUDA(cudaStreamSynchronize(st));
     const McCounters& c = *s.host;
     if (c.flags & kMcBadIndex)
@@ -1400,6 +1467,95 @@ th_status th_context_stage_times(const th_context* ctx, th_stage_times* out)
 int64_t th_launch_count(void)
 {
     return g_launches.load(std::memory_order_relaxed);
+}
+
+namespace th
+{
+namespace
+{
+
+// 16-byte words, then the tail bytes.  Reads of host memory are latency
+// bound: each thread keeps kCopyUnroll independent 16-byte loads in flight.
+constexpr int kCopyUnroll = 8;
+
+__global__ void __launch_bounds__(256) sm_copy_kernel(const unsigned char* __restrict__ src,
+                                                      unsigned char* __restrict__ dst,
+                                                      int64_t n,
+                                                      int vec)
+{
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const int64_t t0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if (vec)
+    {
+        const int64_t nv = n / 16;
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        uint4* d4 = reinterpret_cast<uint4*>(dst);
+        int64_t i = t0;
+        for (; i + (kCopyUnroll - 1) * stride < nv; i += kCopyUnroll * stride)
+        {
+            uint4 r[kCopyUnroll];
+#pragma unroll
+            for (int k = 0; k < kCopyUnroll; ++k)
+                r[k] = s4[i + k * stride];
+#pragma unroll
+            for (int k = 0; k < kCopyUnroll; ++k)
+                d4[i + k * stride] = r[k];
+        }
+        for (; i < nv; i += stride)
+            d4[i] = s4[i];
+        done = nv * 16;
+    }
+    for (int64_t i = done + t0; i < n; i += stride)
+        dst[i] = src[i];
+}
+
+// The device address of a copy operand: device and managed memory as they
+// are, pinned host memory through its mapping (host = true); nullptr for host
+// memory the device cannot address.
+const void* device_address(const void* p, bool& host)
+{
+    host = false;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+        return p;
+    if (a.type == cudaMemoryTypeHost)
+    {
+        host = true;
+        return a.devicePointer;
+    }
+    return nullptr;
+}
+
+} // namespace
+} // namespace th
+
+th_status th_copy(void* dst, const void* src, int64_t bytes, void* stream)
+{
+    if (bytes < 0 || ((!dst || !src) && bytes > 0))
+        return TH_ERR_INVALID_ARGUMENT;
+    if (bytes == 0)
+        return TH_OK;
+    bool src_host = false, dst_host = false;
+    const void* s = th::device_address(src, src_host);
+    void* d = const_cast<void*>(th::device_address(dst, dst_host));
+    if (!s || !d)
+        return TH_ERR_INVALID_ARGUMENT;
+    const int vec = (reinterpret_cast<uintptr_t>(d) % 16 == 0) && (reinterpret_cast<uintptr_t>(s) % 16 == 0);
+    // A copy to or from host memory runs beside the hull kernels on a few
+    // blocks: on GB300 eight blocks read host memory at ~130 GB/s and six
+    // write it at ~190 GB/s (the link's rate), while a grid over all SMs
+    // slows the concurrent hulls.  Device-to-device copies take every SM.
+    const int grid = src_host ? 8 : dst_host ? 6 : 2 * th::sm_count();
+    th::sm_copy_kernel<<<static_cast<unsigned>(grid), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const unsigned char*>(s), static_cast<unsigned char*>(d), bytes, vec);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError() == cudaSuccess ? TH_OK : TH_ERR_CUDA;
 }
 
 th_status th_visual_hull(th_context* ctx, const th_hull_args* args, void* stream, th_hull_info* info)
@@ -1564,7 +1720,7 @@ th_status th_integral_image(th_context* ctx,
                 TH_CUDA(cudaStreamWaitEvent(st, ctx->sat_aux_done, 0));
             ctx->sat_aux.ensure(static_cast<size_t>(kFlagBytes + sb));
             flag = ctx->sat_aux.as<unsigned int>();
-            TH_CUDA(cudaMemsetAsync(flag, 0, sizeof(unsigned int), st));
+            launch_zero(flag, sizeof(unsigned int), st);
             sc = SatScratch{ static_cast<unsigned char*>(ctx->sat_aux.p) + kFlagBytes };
         }
         launch_integral_image(masks, masks_dtype, batch, height, width, out, st, flag, sc);

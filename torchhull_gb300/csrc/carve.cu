@@ -424,7 +424,7 @@ int grid_for(int64_t work_items, int threads)
 
 void launch_hull_init(const HullPlan& p, cudaStream_t s)
 {
-    TH_CUDA(cudaMemsetAsync(p.ctr, 0, sizeof(DevCounters), s));
+    launch_zero(p.ctr, sizeof(DevCounters), s);
     hull_init_kernel<<<1, 32, 0, s>>>(p);
     TH_LAUNCH_CHECK();
 }

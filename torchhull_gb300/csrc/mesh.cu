@@ -473,23 +473,23 @@ __device__ __forceinline__ uint32_t corner_view_mask(const HullPlan& p, int64_t 
     const int64_t r = int64_t{ 1 } << li;
     const int64_t x0 = gx >> 1, y0 = gy >> 1, z0 = gz >> 1;
     const int64_t x1 = (gx - 1) >> 1, y1 = (gy - 1) >> 1, z1 = (gz - 1) >> 1;
-    const int nx = (x1 != x0 && gx > 0) ? 2 : 1, ny = (y1 != y0 && gy > 0) ? 2 : 1, nz = (z1 != z0 && gz > 0) ? 2 : 1;
+    const bool two_x = x1 != x0 && gx > 0, two_y = y1 != y0 && gy > 0, two_z = z1 != z0 && gz > 0;
+    // up to eight cells, a fixed unrolled pattern of predicated loads (issued together)
     uint32_t m = 0;
-    for (int k = 0; k < nz; ++k)
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
     {
-        const int64_t cz = k ? z1 : z0;
-        if (cz >= r)
-            continue;
-        for (int j = 0; j < ny; ++j)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
         {
-            const int64_t cy = j ? y1 : y0;
-            if (cy >= r)
-                continue;
-            for (int i = 0; i < nx; ++i)
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
             {
-                const int64_t cx = i ? x1 : x0;
-                if (cx < r)
-                    m |= p.cell_masks[cx | (cy << li) | (cz << (2 * li))];
+                const int64_t cx = i ? x1 : x0, cy = j ? y1 : y0, cz = k ? z1 : z0;
+                const bool use = (i == 0 || two_x) && (j == 0 || two_y) && (k == 0 || two_z) && cx < r && cy < r &&
+                                 cz < r;
+                if (use)
+                    m |= __ldg(p.cell_masks + (cx | (cy << li) | (cz << (2 * li))));
             }
         }
     }
@@ -1179,7 +1179,7 @@ void launch_cleanup(const HullPlan& p, cudaStream_t s)
 {
     clear_rows_kernel<<<grid_for(p.R * p.R * p.WR, 256), 256, 0, s>>>(p);
     TH_LAUNCH_CHECK();
-    TH_CUDA(cudaMemsetAsync(p.rowbits, 0, sizeof(uint32_t) * ((p.R * p.R + 31) / 32), s));
+    launch_zero(p.rowbits, sizeof(uint32_t) * ((p.R * p.R + 31) / 32), s);
 }
 
 } // namespace th

@@ -713,7 +713,7 @@ void launch_integral_image(const void* masks,
         plan.vec_in = (W * kElemBytes[dtype]) % run_bytes == 0;
         // the ticket counter and this launch's status words start at zero (row
         // vectors of earlier launches of other shapes may lie where they are now)
-        TH_CUDA(cudaMemsetAsync(base, 0, static_cast<size_t>(kSchedBytes + status_bytes(nbands)), s));
+        launch_zero(base, static_cast<size_t>(kSchedBytes + status_bytes(nbands)), s);
         const bool tma = (reinterpret_cast<uintptr_t>(masks) % 16 == 0) && ((W * kElemBytes[dtype]) % 16 == 0);
         const bool ok = dispatch_image_dtype(dtype, [&]<int DT>() {
             if (tma)

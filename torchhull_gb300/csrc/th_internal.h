@@ -46,6 +46,11 @@ int sm_count();
 // cover the work, at most 8 resident blocks per SM.
 int grid_for(int64_t work_items, int threads);
 
+// Zeroes `bytes` of device memory with a kernel (capi.cu): the per-request
+// clears of the pipeline must not wait behind a caller's bulk copies, which a
+// copy-engine memset could.
+void launch_zero(void* p, size_t bytes, cudaStream_t s);
+
 // Scratch of the single-pass integral image (sat.cu): device memory of at
 // least sat_scratch_bytes(B, H, W, dtype) bytes (each launch clears what it needs).
 struct SatScratch

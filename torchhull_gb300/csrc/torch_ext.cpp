@@ -584,6 +584,22 @@ void set_field_ones(int device, bool enable)
     check(th_context_set_option(dc.ctx, TH_OPTION_FIELD_ONES, enable ? 1 : 0), dc.ctx);
 }
 
+// Copies src into dst (same byte size, both contiguous, each a CUDA tensor or
+// a pinned CPU tensor) with a kernel on the current stream of the CUDA side.
+void copy_on_sms(at::Tensor& dst, const at::Tensor& src)
+{
+    TORCH_CHECK(dst.is_contiguous() && src.is_contiguous(), "copy_on_sms: tensors must be contiguous");
+    const int64_t bytes = dst.numel() * static_cast<int64_t>(dst.element_size());
+    TORCH_CHECK(bytes == src.numel() * static_cast<int64_t>(src.element_size()), "copy_on_sms: sizes differ");
+    TORCH_CHECK(dst.is_cuda() || src.is_cuda(), "copy_on_sms: one side must be a CUDA tensor");
+    TORCH_CHECK(dst.is_cuda() || dst.is_pinned(), "copy_on_sms: a CPU destination must be pinned");
+    TORCH_CHECK(src.is_cuda() || src.is_pinned(), "copy_on_sms: a CPU source must be pinned");
+    const at::Tensor& dev = dst.is_cuda() ? dst : src;
+    at::cuda::CUDAGuard guard(dev.device());
+    const th_status st = th_copy(dst.data_ptr(), src.data_ptr(), bytes, stream_of(dev));
+    TORCH_CHECK(st == TH_OK, "copy_on_sms: ", th_status_string(st));
+}
+
 void set_sat_single_pass(int device, bool enable)
 {
     DeviceContext& dc = context_for(device);
@@ -714,6 +730,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m)
           "Field: skip the mask reads of samples whose 2x2 footprint is all ones (default on).");
     m.def("set_field_masks", &set_field_masks, "device"_a, "enable"_a,
           "Field: skip the (corner, view) pairs whose factor the carve proved to be 1 (default on).");
+    m.def("copy_on_sms", &copy_on_sms, "dst"_a, "src"_a,
+          "Copy between a CUDA tensor and a pinned CPU (or CUDA) tensor with a kernel on the current stream.");
     m.def("set_sat_single_pass", &set_sat_single_pass, "device"_a, "enable"_a,
           "Integral images of 0/1 masks in one banded pass (default on).");
     m.def("set_graphs", &set_graphs, "device"_a, "enable"_a,
