@@ -267,8 +267,11 @@ def host_copy(th, method: str):
     """The copy the end-to-end legs move their bytes with, on the current stream: "sm" is
     torchhull_gb300's copy kernel (th_copy: a few blocks of SMs over the pinned buffers' device
     mappings), "dma" is cudaMemcpyAsync (a copy engine).  With copy-engine copies overlapping the
-    hulls, about one loop of three on GB300 lost ~70-80 ms to a stall (either direction alone
-    was enough); the copy kernel showed none in 40 loops and ran ~5% below the stall-free loops."""
+    hulls, about one loop of three on GB300 lost ~70-80 ms to a stall (raw cudaMemcpyAsync as well
+    as torch's copies, either direction alone was enough).  Plain hulls: the copy kernel showed no
+    stall in 40 loops and ran ~5% below the stall-free copy-engine loops.  Batched hulls: its few
+    blocks find little room beside the persistent carve kernel (~232 against ~342 hulls/s for
+    stall-free copy-engine loops), so that leg keeps the copy engines."""
     if method == "sm":
         return th._C.copy_on_sms
 
@@ -463,7 +466,7 @@ def run_gb300(args) -> dict | None:
     copies = torch.cuda.Stream(dev)
     ready = [torch.cuda.Event() for _ in range(2)]
     free = [torch.cuda.Event() for _ in range(2)]
-    xfer = host_copy(th, args.e2e_copy)
+    xfer = host_copy(th, args.e2e_batched_copy)
 
     def batch_in(k):
         s = k % 2
@@ -577,7 +580,7 @@ def run_gb300(args) -> dict | None:
         "e2e_batched": {"value": e2e_batched, "unit": "hulls/s",
                         "path": "th_visual_hull_batch per step; on one side stream the previous step's meshes out, "
                                 "then the next step's inputs in, overlapping the batch",
-                        "allocator_in_timed_loop": e2e_batched_alloc},
+                        "copy_method": args.e2e_batched_copy, "allocator_in_timed_loop": e2e_batched_alloc},
         "roofline": {"bound": "hbm", "kernel": dom[1], "stage": dom[0], "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes": dom[3], "ms": dom[2], "traffic": NCU_TRAFFIC.get(dom[0]),
@@ -1023,7 +1026,10 @@ def main() -> None:
     ap.add_argument("--no-hetero", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--e2e-copy", choices=["dma", "sm"], default="sm",
-                    help="end-to-end legs: host <-> device copies by copy engines or by the copy kernel")
+                    help="plain end-to-end leg: host <-> device copies by the copy kernel or by copy engines")
+    ap.add_argument("--e2e-batched-copy", choices=["dma", "sm"], default="dma",
+                    help="batched end-to-end leg: copy engines (the copy kernel's few blocks starve beside "
+                         "the batch's persistent carve kernel)")
     ap.add_argument("--batch-route", choices=["on", "off"], default="off",
                     help="batched form: requests that fill the GPU alone through the per-request pipeline")
     ap.add_argument("--field-ones", choices=["on", "off"], default="on",
