@@ -267,8 +267,8 @@ def host_copy(th, method: str):
     """The copy the end-to-end legs move their bytes with, on the current stream: "sm" is
     torchhull_gb300's copy kernel (th_copy: a few blocks of SMs over the pinned buffers' device
     mappings), "dma" is cudaMemcpyAsync (a copy engine).  With copy-engine copies overlapping the
-    hulls, about one loop of three on GB300 lost ~70-80 ms to a stall (raw cudaMemcpyAsync as well
-    as torch's copies, either direction alone was enough).  Plain hulls: the copy kernel showed no
+    hulls, about one loop of three on GB300 lost ~70-80 ms: a few consecutive copies ran at a
+    tenth of their rate (raw cudaMemcpyAsync as well as torch's copies, either direction).  Plain hulls: the copy kernel showed no
     stall in 40 loops and ran ~5% below the stall-free copy-engine loops.  Batched hulls: its few
     blocks find little room beside the persistent carve kernel (~232 against ~342 hulls/s for
     stall-free copy-engine loops), so that leg keeps the copy engines."""

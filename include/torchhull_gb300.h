@@ -345,8 +345,9 @@ int64_t th_launch_count(void);
  * (8 blocks when reading host memory, 6 when writing it, all SMs for device
  * to device), sized to overlap the hull kernels.  On GB300, a loop overlapping
  * hulls with cudaMemcpyAsync copies of their inputs and meshes lost ~70-80 ms
- * in about one run of three; the same loop with this kernel showed no such
- * stall in 40 runs and ran ~5% below the stall-free copy-engine runs. */
+ * in about one run of three (a few consecutive copies at a tenth of their
+ * rate); the same loop with this kernel showed no such stall in 40 runs and
+ * ran ~5% below the stall-free copy-engine runs. */
 th_status th_copy(void* dst, const void* src, int64_t bytes, void* stream);
 
 #ifdef __cplusplus
