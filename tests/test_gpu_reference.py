@@ -79,6 +79,9 @@ SCENES = {
                                                       device=dev),
     "cv_partial_256_l7": lambda dev: scenes.make_request(26, 16, 256, 7, True, convention="opencv", device=dev),
     "gl_partial_1024_l9": lambda dev: scenes.partial_request(dev),
+    # more than 32 views: views 32.. are evaluated without inherited view masks
+    "gl_partial_320_l7_40v": lambda dev: scenes.make_request(27, 40, 320, 7, True, device=dev),
+    "cv_full_256_l7_48v": lambda dev: scenes.make_request(28, 48, 256, 7, False, convention="opencv", device=dev),
 }
 
 
@@ -113,14 +116,15 @@ def test_hull_matches_reference(th, ref, scene_cache, name, unique):
 
 
 @pytest.mark.parametrize("name", ["gl_full_256_l6", "gl_partial_192_l6", "cv_full_160_l6", "cv_partial_256_l7",
-                                  "gl_partial_1024_l9"])
+                                  "gl_partial_1024_l9", "gl_partial_320_l7_40v"])
 def test_oracle_matches_reference(ref, scene_cache, name):
     r = scene_cache(name)
     assert_hull_equal(oracle_hull(r), ref_hull(ref, r), f"oracle {name}")
 
 
 @pytest.mark.parametrize("mode", [1, 2])
-@pytest.mark.parametrize("name", ["gl_partial_1024_l9", "gl_full_256_l6", "cv_partial_256_l7"])
+@pytest.mark.parametrize("name", ["gl_partial_1024_l9", "gl_full_256_l6", "cv_partial_256_l7", "gl_partial_320_l7_40v",
+                                  "cv_full_256_l7_48v"])
 def test_forced_carve_kernels_match_reference(th, ref, scene_cache, name, mode):
     """Both carve kernels (views over lanes; (parent, view) items with inherited skip masks), each forced."""
     r = scene_cache(name)
@@ -136,6 +140,21 @@ def test_forced_carve_kernels_match_reference(th, ref, scene_cache, name, mode):
 def test_batched_partial_workload_matches_reference(th, ref, cuda):
     """Four seeded requests of the 32 x 1024^2 level-9 partial workload through the persistent batched carve."""
     reqs = [scenes.partial_request(cuda, seed=3 + i) for i in range(4)]
+    got = th._C.visual_hull_batch([_args(r) for r in reqs])
+    torch.cuda.synchronize()
+    for i, (r, (v, f)) in enumerate(zip(reqs, got, strict=True)):
+        wv, wf = ref.visual_hull(*_args(r))
+        torch.cuda.synchronize()
+        assert torch.equal(f, wf), i
+        assert torch.equal(v.view(torch.int32), wv.view(torch.int32)), i
+
+
+def test_heterogeneous_batch_matches_reference(th, ref, cuda):
+    """A batch of the heterogeneous distribution (views 4..48, sides 256..1024, levels 6..9, partial
+    or full) without its 1024^2 level-9 requests, through the persistent batched carve."""
+    reqs = [r for r in scenes.batched_requests(count=16, seed=5, device=cuda)
+            if not (r.level == 9 and r.masks.shape[1] == 1024)][:12]
+    assert any(r.masks.shape[0] > 32 for r in reqs)
     got = th._C.visual_hull_batch([_args(r) for r in reqs])
     torch.cuda.synchronize()
     for i, (r, (v, f)) in enumerate(zip(reqs, got, strict=True)):
@@ -169,7 +188,7 @@ def test_blur_hull_oracle_matches_reference(ref, blur_scene):
     assert_hull_equal(oracle_hull(r, masks=ref_blurred), ref_hull(ref, r, masks=ref_blurred), "oracle blur + hull")
 
 
-@pytest.mark.parametrize("name", ["gl_full_256_l6", "gl_partial_192_l6", "cv_partial_256_l7"])
+@pytest.mark.parametrize("name", ["gl_full_256_l6", "gl_partial_192_l6", "cv_partial_256_l7", "gl_partial_320_l7_40v"])
 def test_field_matches_reference(th, ref, scene_cache, name):
     r = scene_cache(name)
     args = _args(r)[:7]
