@@ -336,10 +336,11 @@ th_status th_context_stage_times(const th_context* ctx, th_stage_times* out);
 /* Number of kernels this library has launched in this process (all contexts). */
 int64_t th_launch_count(void);
 
-/* Copies `bytes` from src to dst with a kernel on `stream` (no reference
- * counterpart).  Each pointer is device or managed memory, or pinned host
- * memory (cudaHostAlloc, or cudaHostRegister with a device mapping), which is
- * reached through its device mapping; other host memory is
+/* Copies `bytes` from src to dst with a kernel on `stream`, a stream of the
+ * current device (no reference counterpart).  Each pointer is memory of the
+ * current device, managed memory, or pinned host memory (cudaHostAlloc, or
+ * cudaHostRegister with a device mapping), which is reached through its device
+ * mapping; other host memory and other devices' memory are
  * TH_ERR_INVALID_ARGUMENT.
  * The transfer runs on a few blocks of SMs instead of a DMA copy engine
  * (8 blocks when reading host memory, 6 when writing it, all SMs for device

@@ -50,5 +50,8 @@ def test_rejects(C):
         C.copy_on_sms(dev, torch.zeros(64, dtype=torch.uint8))
     with pytest.raises(RuntimeError, match="sizes differ"):
         C.copy_on_sms(dev, torch.zeros(63, dtype=torch.uint8).pin_memory())
+    if torch.cuda.device_count() > 1:
+        with pytest.raises(RuntimeError, match="one device"):
+            C.copy_on_sms(dev, torch.empty(64, dtype=torch.uint8, device="cuda:1"))
     with pytest.raises(RuntimeError, match="CUDA"):
         C.copy_on_sms(torch.zeros(64, dtype=torch.uint8).pin_memory(), torch.zeros(64, dtype=torch.uint8).pin_memory())

@@ -1510,20 +1510,24 @@ __global__ void __launch_bounds__(256) sm_copy_kernel(const unsigned char* __res
         dst[i] = src[i];
 }
 
-// The device address of a copy operand: device and managed memory as they
-// are, pinned host memory through its mapping (host = true); nullptr for host
-// memory the device cannot address.
+// The device address of a copy operand for a kernel on the current device:
+// its own device memory and managed memory as they are, pinned host memory
+// through its mapping (host = true); nullptr for another device's memory and
+// for host memory the device cannot address.
 const void* device_address(const void* p, bool& host)
 {
     host = false;
     cudaPointerAttributes a{};
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    int current = -1;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess || cudaGetDevice(&current) != cudaSuccess)
     {
         cudaGetLastError();
         return nullptr;
     }
-    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+    if (a.type == cudaMemoryTypeManaged)
         return p;
+    if (a.type == cudaMemoryTypeDevice)
+        return a.device == current ? p : nullptr;
     if (a.type == cudaMemoryTypeHost)
     {
         host = true;

@@ -594,6 +594,8 @@ void copy_on_sms(at::Tensor& dst, const at::Tensor& src)
     TORCH_CHECK(dst.is_cuda() || src.is_cuda(), "copy_on_sms: one side must be a CUDA tensor");
     TORCH_CHECK(dst.is_cuda() || dst.is_pinned(), "copy_on_sms: a CPU destination must be pinned");
     TORCH_CHECK(src.is_cuda() || src.is_pinned(), "copy_on_sms: a CPU source must be pinned");
+    TORCH_CHECK(!(dst.is_cuda() && src.is_cuda()) || dst.device() == src.device(),
+                "copy_on_sms: both CUDA tensors must be on one device");
     const at::Tensor& dev = dst.is_cuda() ? dst : src;
     at::cuda::CUDAGuard guard(dev.device());
     const th_status st = th_copy(dst.data_ptr(), src.data_ptr(), bytes, stream_of(dev));
